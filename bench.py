@@ -1,0 +1,298 @@
+"""Assembly benchmark: second-order Nédélec E/B assembly of the 80³ Kuhn unit cube.
+
+Workload (the reference's assembly micro-benchmark): unit cube, 80³ hexes × 6
+Kuhn tets (3,072,000 tets), interior vertices jittered by U[-0.15h, 0.15h]
+(numpy default_rng(0)); per tet εr ~ U[1,10], tanδ ~ U[0.001,0.02]
+(default_rng(1)), μr = 1.  One step = assembling the complex128 curl-curl (E)
+and mass (B) CSR matrices, i.e. tet_mass_stiffness_matrices
+(fem/physics/edm/optimized_assembly.py:43-64).  The CSR pattern is built once
+per mesh before timing (reported separately as ``plan_s``).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--n 80] [--impl reference]
+
+Prints one JSON line.  ``value``: tets/s with inputs resident in HBM (each step
+writes 27.5 GB of values, far more than the 129 MB L2, so no L2 flush is
+needed).  ``e2e``: the same through the C-ABI host entry point
+(emg_assemble_tet_host), with the material H2D and the E/B D2H inside the timed
+region.  ``--impl reference`` times the reference's CPU algorithm (the oracle's
+C++ restatement of the Numba element loop on all host cores + SciPy
+coo_matrix(...).tocsr()) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "assembly tets/s (E+B complex128 CSR, 2nd-order Nedelec)"
+C0 = 299792458.0
+
+
+def make_workload(n: int):
+    from emerge_gb300.mesh import Nedelec2Basis, unit_cube
+    m = unit_cube(n, jitter=0.15, seed=0)
+    field = Nedelec2Basis(m)
+    rng = np.random.default_rng(1)
+    nT = m.n_tets
+    er_s = rng.uniform(1.0, 10.0, nT) * (1 - 1j * rng.uniform(0.001, 0.02, nT))
+    return m, field, er_s.astype(np.complex128)
+
+
+def dense_materials(er_s: np.ndarray):
+    nT = er_s.shape[0]
+    er = np.zeros((3, 3, nT), dtype=np.complex128)
+    ur = np.zeros((3, 3, nT), dtype=np.complex128)
+    for k in range(3):
+        er[k, k] = er_s
+        ur[k, k] = 1.0
+    return er, ur
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(n: int):
+    """DRAM bytes per fill launch from the committed ncu summary (scaled by tets), or None."""
+    p = os.path.join(ROOT, "profiles", "assembly_fill_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return float(d["dram_bytes_per_tet"]) * 6 * n ** 3
+
+
+def cpu_reference(field, er_s, max_tets: int):
+    """Oracle (C++ restatement of _matrix_builder, OpenMP) + SciPy tocsr on a leading slice of tets."""
+    import oracle
+    from scipy.sparse import coo_matrix
+    nT = min(max_tets, field.mesh.n_tets)
+    er, ur = dense_materials(er_s)
+    N = field.n_field
+    t0 = time.perf_counter()
+    dE, dB, rows, cols = oracle.matrix_builder(field, er, ur, 0, nT)
+    t1 = time.perf_counter()
+    E = coo_matrix((dE, (rows, cols)), shape=(N, N)).tocsr()
+    B = coo_matrix((dB, (rows, cols)), shape=(N, N)).tocsr()
+    t2 = time.perf_counter()
+    del E, B
+    return nT, t1 - t0, t2 - t1
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    n = args.n
+    m, field, er_s = make_workload(n)
+    cores = os.cpu_count()
+    sample = args.cpu_sample
+    for _ in range(args.warmup):
+        cpu_reference(field, er_s, min(sample, 20000))
+    times = []
+    nts = None
+    for _ in range(args.steps):
+        nts, ti, tc = cpu_reference(field, er_s, sample)
+        times.append(ti + tc)
+    t = sum(times) / len(times)
+    v = nts / t
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "tets/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": f"assembly {n}^3 Kuhn unit cube, jitter 0.15h, eps U[1,10] tan U[.001,.02], mu=1",
+                   "tets": int(m.n_tets), "n_field": int(field.n_field), "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": v, "unit": "tets/s", "cores": cores, "kind": "port",
+                         "sample": f"first {nts} tets of the {n}^3 mesh per step: C++/OpenMP restatement of "
+                                   f"_matrix_builder + scipy coo.tocsr (Numba is not available)"},
+        "e2e": {"value": v, "unit": "tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from emerge_gb300 import _build
+    from emerge_gb300.assembly import AssemblyPlan, material_scalars
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    _build.build()
+    n = args.n
+    m, field, er_s = make_workload(n)
+    er, ur = dense_materials(er_s) if n <= 40 else (None, None)
+    eps = er_s
+    mu_inv = np.ones(m.n_tets, dtype=np.complex128)
+    if er is not None:
+        eps, mu_inv = material_scalars(er, ur)
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    plan = AssemblyPlan(field, dev)
+    torch.cuda.synchronize()
+    plan_s = time.perf_counter() - t0
+    e = torch.as_tensor(eps, device=dev)
+    mi = torch.as_tensor(mu_inv, device=dev)
+    E = torch.empty(plan.nnz, dtype=torch.complex128, device=dev)
+    B = torch.empty(plan.nnz, dtype=torch.complex128, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        plan.assemble(e, mi, E, B)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t_begin = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_begin.record(stream)
+        for k in range(args.steps):
+            starts[k].record(stream)
+            plan.assemble(e, mi, E, B)
+            ends[k].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        time.sleep(0.3)
+    total_ms = t_begin.elapsed_time(t_end)
+    launch_ms = [s.elapsed_time(x) for s, x in zip(starts, ends)]
+    ms = total_ms / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * m.n_tets / (ms / 1e3)
+
+    # end to end through the host entry point: materials H2D + E/B D2H inside the timed region
+    pin_E = torch.empty(plan.nnz, dtype=torch.complex128, pin_memory=True)
+    pin_B = torch.empty(plan.nnz, dtype=torch.complex128, pin_memory=True)
+    pin_eps = torch.as_tensor(eps).pin_memory()
+    pin_mu = torch.as_tensor(mu_inv).pin_memory()
+    npE, npB = pin_E.numpy(), pin_B.numpy()
+    npe, npm = pin_eps.numpy(), pin_mu.numpy()
+    for _ in range(max(1, min(args.warmup, 2))):
+        plan.assemble_host(npe, npm, npE, npB)
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        plan.assemble_host(npe, npm, npE, npB)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_val = world * m.n_tets / e2e_s
+
+    nnz, nT, nN = plan.nnz, m.n_tets, m.n_nodes
+    alg_bytes = 2 * 16 * nnz + 4 * nnz + nT * (20 * 4 + 4 * 4 + 16 + 16) + 24 * nN
+    kern_s = statistics.median(launch_ms) / 1e3
+    achieved = alg_bytes / kern_s / 1e9
+    peak, peak_kind = peaks()
+    out = {
+        "metric": METRIC, "value": value, "unit": "tets/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (complex128 values)", "data": "synthetic",
+        "config": {"workload": f"assembly {n}^3 Kuhn unit cube, jitter 0.15h, eps U[1,10] tan U[.001,.02], mu=1",
+                   "tets": int(nT), "n_field": int(plan.n_field), "nnz_per_matrix": int(nnz),
+                   "l2": "no flush: each step writes 32*nnz bytes >> 129 MB L2", "parallelism": f"replicas x{world}",
+                   "plan_s": round(plan_s, 3)},
+        "e2e": {"value": e2e_val, "unit": "tets/s", "h2d_bytes_per_step": int(2 * 16 * nT),
+                "d2h_bytes_per_step": int(2 * 16 * nnz), "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "kernel": "k_fill",
+                     "algorithmic_bytes_per_launch": int(alg_bytes), "traffic": traffic_per_launch(n)},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        nts, ti, tc = cpu_reference(field, er_s, args.cpu_sample)
+        out["cpu_baseline"] = {"value": nts / (ti + tc), "unit": "tets/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"first {nts} tets of the same mesh: C++/OpenMP restatement of the "
+                                         f"reference element loop ({ti:.2f} s) + scipy coo.tocsr ({tc:.2f} s)"}
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--n", type=int, default=80, help="hexes per cube side (80 -> 3.07M tets)")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=200_000, help="tets in the bounded CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,73 @@
+"""ctypes binding of the C ABI in include/emerge_gb300.h.
+
+The shared library is built in-tree (``emerge_gb300/libemerge_gb300.so``, see
+``_build.py``).  There is no CPU fallback: if the library is missing or a call
+fails, an exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libemerge_gb300.so")
+
+c_i64 = ctypes.c_int64
+c_i32p = ctypes.POINTER(ctypes.c_int32)
+c_i64p = ctypes.POINTER(ctypes.c_int64)
+c_f64p = ctypes.POINTER(ctypes.c_double)
+c_vp = ctypes.c_void_p
+
+# name -> (restype, argtypes); mirrors include/emerge_gb300.h
+SIGNATURES = {
+    "emg_last_error": (ctypes.c_char_p, []),
+    "emg_version": (ctypes.c_char_p, []),
+    "emg_plan_create": (ctypes.c_int, [c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                       c_vp, ctypes.POINTER(c_vp)]),
+    "emg_plan_nnz": (c_i64, [c_vp]),
+    "emg_plan_pattern": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp]),
+    "emg_assemble_tet": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "emg_assemble_tet_host": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "emg_plan_destroy": (None, [c_vp]),
+}
+
+
+class EmgError(RuntimeError):
+    """A C-ABI call returned a nonzero status."""
+
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed (status {code}): {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load (once) and return the shared library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library not built: {path} is missing (run __graft_entry__.build() or "
+                           f"python -m emerge_gb300._build)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(fn: str, code: int) -> None:
+    if code != 0:
+        msg = load().emg_last_error()
+        raise EmgError(fn, code, msg.decode() if msg else "")
+
+
+def call(fn: str, *args):
+    """Call ``fn`` and raise EmgError on a nonzero status."""
+    code = getattr(load(), fn)(*args)
+    check(fn, code)
+    return code

@@ -1,0 +1,274 @@
+"""Generate the golden fixtures in tests/golden/ by running the EMerge reference.
+
+Run in a checkout that has the reference at /root/reference:
+
+    python tests/golden/make_golden.py
+
+The reference runs unmodified behind the import shims of ``_refshim`` (Numba
+kernels execute as plain Python, gmsh is replaced by a fake that serves the
+project's structured meshes).  Every fixture records the exact inputs the
+reference saw, so the tests can replay them through the oracle and through the
+CUDA path without the reference being present.
+
+Fixtures:
+  tet_elements.npz   ned2_tet_stiff_mass on 48 tets (fem/mth/tet.py:854-1088)
+  tri_elements.npz   ned2_tri_stiff_force / ned2_tri_stiff (fem/mth/tri.py:575-797)
+  small_assembly.npz tet_mass_stiffness_matrices on a 2x2x2-hex box, two material sets
+                     (fem/physics/edm/optimized_assembly.py:43-116)
+  waveguide.npz      WR-90 straight guide, h = 3 mm, 10 GHz: K row checksums, port
+                     vectors, solve_ids, SuperLU field and S-parameters
+                     (fem/physics/edm/assembler.py:312-388, fem/solver.py:405-469,
+                     fem/physics/edm/emfreq3d.py:607-779)
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import _refshim  # noqa: E402
+
+GMSH = _refshim.install()
+
+from fem.mth import tet as ref_tet  # noqa: E402
+from fem.mth import tri as ref_tri  # noqa: E402
+from fem.mth import optimized as ref_opt  # noqa: E402
+from fem import mesh3d as ref_mesh3d  # noqa: E402
+from fem.elements.nedelec2 import Nedelec2  # noqa: E402
+from fem.physics.edm import optimized_assembly as ref_asm  # noqa: E402
+from fem.physics.edm import assembler as ref_assembler  # noqa: E402
+from fem.physics.edm.emfreq3d import Electrodynamics3D  # noqa: E402
+from fem import solver as ref_solver  # noqa: E402
+from fem import bc as ref_bc  # noqa: E402
+from fem.cs import CoordinateSystem, Axis  # noqa: E402
+from fem.selection import FaceSelection  # noqa: E402
+
+from emerge_gb300.mesh import structured_box, TET_EDGE_SLOTS, TET_FACE_SLOTS  # noqa: E402
+from emerge_gb300 import mesh as pm  # noqa: E402
+
+C0 = 299792458
+
+
+def _local_maps(gid):
+    """local_edge_map / local_tri_map of a tet whose vertices have global ids ``gid``."""
+    ge = np.array([[min(gid[p], gid[q]), max(gid[p], gid[q])] for p, q in TET_EDGE_SLOTS.T]).T
+    gf = np.array([sorted([gid[a], gid[b], gid[c]]) for a, b, c in TET_FACE_SLOTS.T]).T
+    lem = ref_opt.local_mapping(np.asarray(gid, dtype=np.int64), ge.astype(np.int64))
+    ltm = ref_opt.local_mapping(np.asarray(gid, dtype=np.int64), gf.astype(np.int64))
+    return lem, ltm
+
+
+def _rand_c3(rng, iso):
+    if iso:
+        return (rng.uniform(0.5, 10) - 1j * rng.uniform(0, 0.2)) * np.eye(3, dtype=np.complex128)
+    return (rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3)) * 0.3 + 3 * np.eye(3)).astype(np.complex128)
+
+
+def make_tet_elements():
+    rng = np.random.default_rng(1234)
+    n = 48
+    verts = np.zeros((n, 3, 4))
+    lens = np.zeros((n, 6))
+    lem = np.zeros((n, 2, 6), dtype=np.int64)
+    ltm = np.zeros((n, 3, 4), dtype=np.int64)
+    Ms = np.zeros((n, 3, 3), dtype=np.complex128)
+    Mm = np.zeros((n, 3, 3), dtype=np.complex128)
+    D = np.zeros((n, 20, 20), dtype=np.complex128)
+    F = np.zeros((n, 20, 20), dtype=np.complex128)
+    for k in range(n):
+        scale = [1.0, 1e-3, 3e-3, 0.0125][k % 4]
+        offset = [0.0, 0.0, 0.02, 0.9][k % 4]
+        v = offset + scale * (np.array([[0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1]], dtype=float)
+                              + 0.3 * rng.uniform(-1, 1, size=(3, 4)))
+        gid = rng.choice(1000, size=4, replace=False)
+        lem[k], ltm[k] = _local_maps(gid)
+        verts[k] = v
+        for s, (p, q) in enumerate(TET_EDGE_SLOTS.T):
+            lens[k, s] = np.sqrt(np.sum((v[:, p] - v[:, q]) ** 2))
+        Ms[k] = _rand_c3(rng, k % 3 != 2)
+        Mm[k] = _rand_c3(rng, k % 3 != 1)
+        D[k], F[k] = ref_tet.ned2_tet_stiff_mass(verts[k], lens[k], lem[k], ltm[k], Ms[k], Mm[k])
+    np.savez_compressed(os.path.join(HERE, "tet_elements.npz"), verts=verts, edge_lengths=lens,
+                        local_edge_map=lem, local_tri_map=ltm, Ms=Ms, Mm=Mm, D=D, F=F)
+    print("tet_elements: ok")
+
+
+def make_tri_elements():
+    rng = np.random.default_rng(99)
+    n = 24
+    DPTs = ref_opt.gaus_quad_tri(4)
+    lv = np.zeros((n, 3, 3))
+    gam = np.zeros(n, dtype=np.complex128)
+    U = np.zeros((n, 3, DPTs.shape[1]), dtype=np.complex128)
+    Bf = np.zeros((n, 8, 8), dtype=np.complex128)
+    bf = np.zeros((n, 8), dtype=np.complex128)
+    v3 = np.zeros((n, 3, 3))
+    el = np.zeros((n, 3))
+    Bs = np.zeros((n, 8, 8), dtype=np.complex128)
+    for k in range(n):
+        s = [1e-3, 2e-3, 1.0][k % 3]
+        lv[k] = s * (np.array([[0, 1, 0], [0, 0, 1], [0, 0, 0]], dtype=float) + 0.3 * rng.uniform(-1, 1, (3, 3)))
+        lv[k, 2] = rng.uniform(-1, 1, 3) * s * 0.01
+        gam[k] = 1j * rng.uniform(50, 300) + rng.uniform(-1, 1)
+        U[k] = rng.normal(size=(3, DPTs.shape[1])) + 1j * rng.normal(size=(3, DPTs.shape[1]))
+        Bf[k], bf[k] = ref_tri.ned2_tri_stiff_force(lv[k], gam[k], U[k], DPTs)
+        v3[k] = s * (np.eye(3) + 0.3 * rng.uniform(-1, 1, (3, 3))) + rng.uniform(-1, 1, (3, 1)) * s
+        el[k] = [np.linalg.norm(v3[k][:, a] - v3[k][:, b]) for a, b in ((0, 1), (1, 2), (0, 2))]
+        Bs[k] = ref_tri.ned2_tri_stiff(v3[k], el[k], gam[k])
+    np.savez_compressed(os.path.join(HERE, "tri_elements.npz"), lcs_vertices=lv, gamma=gam, Uinc=U,
+                        DPTs=DPTs, B_force=Bf, b_force=bf, vertices=v3, edge_lengths=el, B_stiff=Bs)
+    print("tri_elements: ok")
+
+
+def reference_mesh(tm):
+    """Run the reference Mesh3D.update on a project mesh through the fake gmsh."""
+    GMSH.set_mesh(tm.nodes, tm.tets, tm.boundary, tm.cell_tag)
+    m = ref_mesh3d.Mesh3D(None)
+    m.update()
+    return m
+
+
+def mesh_arrays(m, prefix=""):
+    return {prefix + "nodes": m.nodes, prefix + "tets": m.tets.astype(np.int32),
+            prefix + "edges": m.edges.astype(np.int32), prefix + "tris": m.tris.astype(np.int32),
+            prefix + "tet_to_edge": m.tet_to_edge.astype(np.int32),
+            prefix + "tet_to_tri": m.tet_to_tri.astype(np.int32),
+            prefix + "tri_to_edge": m.tri_to_edge.astype(np.int32),
+            prefix + "tri_to_tet": m.tri_to_tet.astype(np.int32),
+            prefix + "edge_lengths": m.edge_lengths}
+
+
+def make_small_assembly():
+    rng = np.random.default_rng(7)
+    xs = np.array([0.0, 0.4, 1.0])
+    tm = structured_box(xs, xs * 0.8, xs * 1.3 + 0.5, jitter=0.15, seed=3)
+    m = reference_mesh(tm)
+    field = Nedelec2(m)
+    nT = m.n_tets
+    out = mesh_arrays(m)
+    out["tet_to_field"] = field.tet_to_field.astype(np.int32)
+    for tag, iso_mu in (("a", True), ("b", False)):
+        er = np.zeros((3, 3, nT), dtype=np.complex128)
+        ur = np.zeros((3, 3, nT), dtype=np.complex128)
+        for t in range(nT):
+            er[:, :, t] = rng.uniform(1, 10) * (1 - 1j * rng.uniform(0.001, 0.02)) * np.eye(3)
+            ur[:, :, t] = np.eye(3) if iso_mu else rng.uniform(0.5, 3) * np.eye(3)
+        t0 = time.time()
+        E, B = ref_asm.tet_mass_stiffness_matrices(field, er, ur)
+        print(f"small_assembly[{tag}]: {nT} tets in {time.time() - t0:.1f} s, N={E.shape[0]}, nnz={E.nnz}")
+        out[f"er_{tag}"] = er
+        out[f"ur_{tag}"] = ur
+        for name, M in (("E", E), ("B", B)):
+            out[f"{name}_{tag}_indptr"] = M.indptr.astype(np.int64)
+            out[f"{name}_{tag}_indices"] = M.indices.astype(np.int32)
+            out[f"{name}_{tag}_data"] = M.data
+    np.savez_compressed(os.path.join(HERE, "small_assembly.npz"), **out)
+
+
+def waveguide_mesh(h=3e-3):
+    a, b, L = 0.02286, 0.01016, 0.05
+    nx, ny, nz = int(np.ceil(a / h)), int(np.ceil(L / h)), int(np.ceil(b / h))
+    return structured_box(np.linspace(0, a, nx + 1), np.linspace(0, L, ny + 1), np.linspace(0, b, nz + 1)), (a, b, L)
+
+
+def make_waveguide():
+    tm, (a, b, L) = waveguide_mesh()
+    m = reference_mesh(tm)
+    field = Nedelec2(m)
+    nT = m.n_tets
+    er = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    ur = er.copy()
+    p1 = ref_bc.RectangularWaveguide(FaceSelection([pm.FACE_YMIN]), 1, cs=CoordinateSystem(
+        Axis(np.array([1.0, 0, 0])), Axis(np.array([0, 0, 1.0])), Axis(np.array([0, -1.0, 0])),
+        np.array([a / 2, 0.0, b / 2])), dims=(a, b))
+    p2 = ref_bc.RectangularWaveguide(FaceSelection([pm.FACE_YMAX]), 2, cs=CoordinateSystem(
+        Axis(np.array([-1.0, 0, 0])), Axis(np.array([0, 0, 1.0])), Axis(np.array([0, 1.0, 0])),
+        np.array([a / 2, L, b / 2])), dims=(a, b))
+    # the reference stores ``dims`` only when it derives them itself (fem/bc.py:538-546)
+    p1.dims = (a, b)
+    p2.dims = (a, b)
+    pec = ref_bc.PEC(FaceSelection([pm.FACE_XMIN, pm.FACE_XMAX, pm.FACE_ZMIN, pm.FACE_ZMAX]))
+    bcs = [pec, p1, p2]
+    asm = ref_assembler.Assembler()
+    freqs = [9.0e9, 10.0e9]
+    routine = ref_solver.SolveRoutine(ref_solver.ReverseCuthillMckee(), ref_solver.Preconditioner(), None,
+                                      ref_solver.SolverSuperLU(), None, None)
+    routine.use_preconditioner = False
+    phys = Electrodynamics3D.__new__(Electrodynamics3D)
+    phys.mesh = m
+    all_ports = [p1, p2]
+    verts = set()
+    for p in all_ports:
+        tris = m.get_triangles(p.tags)
+        p._tri_ids = tris
+        p._tri_vertices = m.tris[:, tris]
+        verts.update(set(p._tri_vertices.ravel().tolist()))
+    port_tets = np.array([t for t in range(nT) if not set(m.tets[:, t].tolist()).isdisjoint(verts)])
+    out = mesh_arrays(m)
+    out["tet_to_field"] = field.tet_to_field.astype(np.int32)
+    out["tri_to_field"] = field.tri_to_field.astype(np.int32)
+    out["freqs"] = np.array(freqs)
+    out["dims"] = np.array([a, b, L])
+    out["port_tris_1"] = p1._tri_ids.astype(np.int32)
+    out["port_tris_2"] = p2._tri_ids.astype(np.int32)
+    out["pec_tris"] = m.get_triangles(pec.tags).astype(np.int32)
+    S = np.zeros((len(freqs), 2, 2), dtype=np.complex128)
+    t0 = time.time()
+    for fi, f in enumerate(freqs):
+        k0 = 2 * np.pi * f / C0
+        K, bvec, solve_ids, pvecs = asm.assemble_freq_matrix(field, er, ur, bcs, f, cache_matrices=True)
+        if fi == 0:
+            E, B = asm.cached_matrices
+            n = E.shape[0]
+            w = (np.arange(n) + 1.0) / n
+            for name, M in (("E", E), ("B", B)):
+                out[f"{name}_nnz"] = np.int64(M.nnz)
+                out[f"{name}_rowsum"] = np.asarray(M.sum(axis=1)).ravel()
+                out[f"{name}_rowmom"] = M @ w
+                out[f"{name}_indptr"] = M.indptr.astype(np.int64)
+            out["solve_ids"] = solve_ids.astype(np.int32)
+        Kc = K.tocsr()
+        out[f"K{fi}_rowsum"] = np.asarray(Kc.sum(axis=1)).ravel()
+        out[f"K{fi}_rowmom"] = Kc @ ((np.arange(Kc.shape[0]) + 1.0) / Kc.shape[0])
+        for pn in (1, 2):
+            nz = np.nonzero(pvecs[pn])[0]
+            out[f"pvec{fi}_{pn}_idx"] = nz.astype(np.int32)
+            out[f"pvec{fi}_{pn}_val"] = pvecs[pn][nz]
+        for active in all_ports:
+            active.active = True
+            sol = routine.solve(K, bvec + pvecs[active.port_number], solve_ids, reuse=False)
+            out[f"x{fi}_{active.port_number}"] = sol
+            fieldf = field.interpolate_Ef(sol, tetids=port_tets)
+            ones = np.ones((3, 3, 0))
+            pf, pmode = phys._compute_s_data(active, fieldf, active._tri_vertices, k0,
+                                             np.repeat(np.eye(3)[:, :, None], len(active._tri_ids), 2),
+                                             np.repeat(np.eye(3)[:, :, None], len(active._tri_ids), 2))
+            for bcp in all_ports:
+                pf, _ = phys._compute_s_data(bcp, fieldf, bcp._tri_vertices, k0,
+                                             np.repeat(np.eye(3)[:, :, None], len(bcp._tri_ids), 2),
+                                             np.repeat(np.eye(3)[:, :, None], len(bcp._tri_ids), 2))
+                S[fi, bcp.port_number - 1, active.port_number - 1] = pf / pmode
+            active.active = False
+        print(f"waveguide f={f / 1e9:.1f} GHz: |S11|={abs(S[fi, 0, 0]):.4f} |S21|={abs(S[fi, 1, 0]):.4f} "
+              f"({time.time() - t0:.1f} s)")
+    out["S"] = S
+    out["port_tets"] = port_tets.astype(np.int32)
+    np.savez_compressed(os.path.join(HERE, "waveguide.npz"), **out)
+
+
+if __name__ == "__main__":
+    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide"]
+    if "tet" in which:
+        make_tet_elements()
+    if "tri" in which:
+        make_tri_elements()
+    if "small" in which:
+        make_small_assembly()
+    if "waveguide" in which:
+        make_waveguide()

@@ -1,0 +1,135 @@
+"""CUDA assembly path (through the C ABI) against the reference fixtures and the oracle.
+
+Tolerance: values within 1e-12 of the largest |value| of their CSR row; the
+pattern (indptr, indices) bit-exact.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from _fixtures import csr_from, field_from, load, rel_to_rowmax
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from emerge_gb300 import _build
+    _build.build()
+    return torch
+
+
+def _random_materials(nT, seed, mu_one=True):
+    rng = np.random.default_rng(seed)
+    er = (rng.uniform(1, 10, nT) * (1 - 1j * rng.uniform(0.001, 0.02, nT)))
+    ur = np.ones(nT, dtype=np.complex128) if mu_one else rng.uniform(0.5, 3, nT) + 0j
+    eye = np.eye(3)[:, :, None]
+    return eye * er[None, None, :], eye * ur[None, None, :]
+
+
+@pytest.mark.parametrize("tag", ["a", "b"])
+def test_small_assembly_matches_reference(torch_cuda, tag):
+    from emerge_gb300.assembly import tet_mass_stiffness_matrices
+    z = load("small_assembly.npz")
+    field = field_from(z)
+    E, B = tet_mass_stiffness_matrices(field, z["er_" + tag], z["ur_" + tag])
+    assert rel_to_rowmax(E, csr_from(z, "E_" + tag)) <= TOL
+    assert rel_to_rowmax(B, csr_from(z, "B_" + tag)) <= TOL
+
+
+def test_waveguide_checksums_match_reference(torch_cuda):
+    from emerge_gb300.assembly import tet_mass_stiffness_matrices
+    z = load("waveguide.npz")
+    field = field_from(z)
+    nT = field.mesh.n_tets
+    eye = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    E, B = tet_mass_stiffness_matrices(field, eye, eye)
+    n = E.shape[0]
+    w = (np.arange(n) + 1.0) / n
+    for name, M in (("E", E), ("B", B)):
+        assert M.nnz == int(z[name + "_nnz"])
+        assert np.array_equal(M.indptr, z[name + "_indptr"])
+        scale = np.abs(M).max(axis=1).toarray().ravel()
+        assert np.max(np.abs(np.asarray(M.sum(axis=1)).ravel() - z[name + "_rowsum"]) / scale) <= TOL
+        assert np.max(np.abs(M @ w - z[name + "_rowmom"]) / scale) <= TOL
+
+
+@pytest.mark.parametrize("n,mu_one", [(6, True), (11, False)])
+def test_jittered_cube_matches_oracle(torch_cuda, n, mu_one):
+    from emerge_gb300.assembly import tet_mass_stiffness_matrices
+    from emerge_gb300.mesh import Nedelec2Basis, unit_cube
+    m = unit_cube(n, jitter=0.15, seed=n)
+    field = Nedelec2Basis(m)
+    er, ur = _random_materials(m.n_tets, n, mu_one)
+    E, B = tet_mass_stiffness_matrices(field, er, ur)
+    Eo, Bo = oracle.tet_mass_stiffness_matrices(field, er, ur)
+    assert rel_to_rowmax(E, Eo) <= TOL
+    assert rel_to_rowmax(B, Bo) <= TOL
+
+
+def test_device_path_is_deterministic(torch_cuda):
+    torch = torch_cuda
+    from emerge_gb300.assembly import AssemblyPlan, material_scalars
+    from emerge_gb300.mesh import Nedelec2Basis, unit_cube
+    m = unit_cube(9, jitter=0.15, seed=1)
+    field = Nedelec2Basis(m)
+    er, ur = _random_materials(m.n_tets, 5)
+    eps, mu_inv = material_scalars(er, ur)
+    plan = AssemblyPlan(field)
+    e = torch.as_tensor(eps, device="cuda")
+    mi = torch.as_tensor(mu_inv, device="cuda")
+    E1, B1 = plan.assemble(e, mi)
+    E2, B2 = plan.assemble(e, mi)
+    torch.cuda.synchronize()
+    assert torch.equal(torch.view_as_real(E1), torch.view_as_real(E2))
+    assert torch.equal(torch.view_as_real(B1), torch.view_as_real(B2))
+    # host entry point gives the same bits as the device entry point
+    Eh, Bh = plan.assemble_host(eps, mu_inv)
+    assert np.array_equal(Eh.view(np.float64), torch.view_as_real(E1).cpu().numpy().ravel())
+    assert np.array_equal(Bh.view(np.float64), torch.view_as_real(B1).cpu().numpy().ravel())
+
+
+def test_empty_mesh_and_boundary_only_entities(torch_cuda):
+    """A single tet: every entity has one incidence; nnz = 20*20."""
+    from emerge_gb300.assembly import tet_mass_stiffness_matrices
+    from emerge_gb300.mesh import Nedelec2Basis, TetMesh
+    nodes = np.array([[0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1]], dtype=float) * 1e-3
+    m = TetMesh(nodes, np.array([[0], [1], [2], [3]]))
+    field = Nedelec2Basis(m)
+    er, ur = _random_materials(1, 3)
+    E, B = tet_mass_stiffness_matrices(field, er, ur)
+    Eo, Bo = oracle.tet_mass_stiffness_matrices(field, er, ur)
+    assert E.nnz == 400
+    assert rel_to_rowmax(E, Eo) <= TOL and rel_to_rowmax(B, Bo) <= TOL
+
+
+def test_bad_mesh_is_rejected(torch_cuda):
+    from emerge_gb300._lib import EmgError
+    from emerge_gb300.assembly import AssemblyPlan
+    from emerge_gb300.mesh import Nedelec2Basis, unit_cube
+    m = unit_cube(2)
+    field = Nedelec2Basis(m)
+    field.tet_to_field = field.tet_to_field.copy()
+    field.tet_to_field[3, 5] = field.n_field + 7          # out of range
+    with pytest.raises(EmgError):
+        AssemblyPlan(field)
+    field = Nedelec2Basis(m)
+    field.tet_to_field = field.tet_to_field.copy()
+    field.tet_to_field[13, 2] += 1                         # mode-2 DOF no longer pairs consistently
+    with pytest.raises(EmgError):
+        AssemblyPlan(field)
+
+
+def test_anisotropic_material_is_rejected(torch_cuda):
+    from emerge_gb300.assembly import tet_mass_stiffness_matrices
+    z = load("small_assembly.npz")
+    field = field_from(z)
+    er = z["er_a"].copy()
+    er[0, 1, 0] = 0.1
+    with pytest.raises(NotImplementedError):
+        tet_mass_stiffness_matrices(field, er, z["ur_a"])
