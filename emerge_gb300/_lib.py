@@ -29,6 +29,7 @@ SIGNATURES = {
     "emg_assemble_tet": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "emg_assemble_tet_host": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "emg_plan_destroy": (None, [c_vp]),
+    "emg_csr_pattern_noalloc": (ctypes.c_int, [c_i64, c_i64, c_vp, c_vp, c_vp, c_i64, c_i64p, c_vp]),
 }
 
 

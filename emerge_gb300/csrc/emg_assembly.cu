@@ -696,3 +696,142 @@ extern "C" int emg_assemble_tet_host(emg_plan* p, const double* eps, const doubl
 }
 
 extern "C" void emg_plan_destroy(emg_plan* p) { free_plan(p); }
+
+// ------------------------------------------------- pattern without allocation ---
+// emg_csr_pattern_noalloc: the CSR pattern builder of emg_plan_create for callers
+// that cannot allocate device memory.  All of its scratch lives in one file-scope
+// device array of fixed size, so the entry point calls no cudaMalloc/cudaFree.
+#include <mutex>
+
+namespace emg {
+namespace {
+
+constexpr int64_t kNoAllocMaxTets = 8192;
+constexpr int64_t kNoAllocMaxField = 65536;
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+// byte offsets of the scratch arrays inside g_noalloc_scratch
+constexpr size_t kOffErr = 0;
+constexpr size_t kOffPartner = align256(kOffErr + sizeof(int));
+constexpr size_t kOffRole = align256(kOffPartner + sizeof(int32_t) * kNoAllocMaxField);
+constexpr size_t kOffCursor = align256(kOffRole + sizeof(int32_t) * kNoAllocMaxField);
+constexpr size_t kOffEntList = align256(kOffCursor + sizeof(int32_t) * kNoAllocMaxField);
+constexpr size_t kOffIncCnt = align256(kOffEntList + sizeof(int32_t) * kNoAllocMaxField);
+constexpr size_t kOffFlag = align256(kOffIncCnt + sizeof(int64_t) * (kNoAllocMaxField + 1));
+constexpr size_t kOffFlagScan = align256(kOffFlag + sizeof(int64_t) * (kNoAllocMaxField + 1));
+constexpr size_t kOffIncPtr = align256(kOffFlagScan + sizeof(int64_t) * (kNoAllocMaxField + 1));
+constexpr size_t kOffRowLen = align256(kOffIncPtr + sizeof(int64_t) * (kNoAllocMaxField + 1));
+constexpr size_t kOffScan = align256(kOffRowLen + sizeof(int64_t) * (kNoAllocMaxField + 1));
+constexpr size_t kScanElems = (kNoAllocMaxField + 1 + 4095) / 4096 + 2;
+constexpr size_t kOffInc = align256(kOffScan + sizeof(int64_t) * kScanElems);
+constexpr size_t kNoAllocBytes = align256(kOffInc + sizeof(int64_t) * 10 * kNoAllocMaxTets);  // ~4.9 MB
+
+// Shared by every call on a device; holds the last call's contents.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[64] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device (looked up once per device).
+int noalloc_scratch(unsigned char** out) {
+    int dev = 0;
+    EMG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("emg_csr_pattern_noalloc: device ordinal >= 64");
+        return EMG_ERR_LIMIT;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_addr[dev] == nullptr) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    return EMG_OK;
+}
+
+}  // namespace
+}  // namespace emg
+
+extern "C" int emg_csr_pattern_noalloc(int64_t n_tets, int64_t n_field, const int32_t* tet_to_field,
+                                       int64_t* indptr, int32_t* indices, int64_t indices_capacity,
+                                       int64_t* nnz_out, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(nnz_out != nullptr && indptr != nullptr, "emg_csr_pattern_noalloc: NULL output pointer");
+    EMG_CHECK_ARG(n_tets >= 0 && n_field >= 0 && indices_capacity >= 0, "emg_csr_pattern_noalloc: negative size");
+    if (n_tets > kNoAllocMaxTets || n_field > kNoAllocMaxField) {
+        set_error("emg_csr_pattern_noalloc: mesh too large for the fixed scratch (at most 8192 tets and 65536 "
+                  "DOFs); use emg_plan_create");
+        return EMG_ERR_LIMIT;
+    }
+    EMG_CHECK_ARG(n_tets == 0 || tet_to_field != nullptr, "emg_csr_pattern_noalloc: NULL tet_to_field");
+    *nnz_out = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char* base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    const int64_t N = n_field;
+    int* d_err = reinterpret_cast<int*>(base + kOffErr);
+    int32_t* partner = reinterpret_cast<int32_t*>(base + kOffPartner);
+    int32_t* role = reinterpret_cast<int32_t*>(base + kOffRole);
+    int32_t* cursor = reinterpret_cast<int32_t*>(base + kOffCursor);
+    int32_t* ent_list = reinterpret_cast<int32_t*>(base + kOffEntList);
+    int64_t* inc_cnt = reinterpret_cast<int64_t*>(base + kOffIncCnt);
+    int64_t* flag = reinterpret_cast<int64_t*>(base + kOffFlag);
+    int64_t* flag_scan = reinterpret_cast<int64_t*>(base + kOffFlagScan);
+    int64_t* inc_ptr = reinterpret_cast<int64_t*>(base + kOffIncPtr);
+    int64_t* row_len = reinterpret_cast<int64_t*>(base + kOffRowLen);
+    int64_t* scan_tmp = reinterpret_cast<int64_t*>(base + kOffScan);
+    int64_t* inc = reinterpret_cast<int64_t*>(base + kOffInc);
+    // the previous call's contents are still there: reset what the build accumulates into
+    EMG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), s));
+    if (N > 0) {
+        EMG_CUDA(cudaMemsetAsync(partner, 0xff, sizeof(int32_t) * N, s));
+        EMG_CUDA(cudaMemsetAsync(role, 0, sizeof(int32_t) * N, s));
+        EMG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * N, s));
+        EMG_CUDA(cudaMemsetAsync(inc_cnt, 0, sizeof(int64_t) * (N + 1), s));
+        EMG_CUDA(cudaMemsetAsync(row_len, 0, sizeof(int64_t) * (N + 1), s));
+    }
+    const int T = 256;
+    if (n_tets > 0) {
+        k_incidence_count<<<grid_for(n_tets * 10, T), T, 0, s>>>(tet_to_field, n_tets, N, partner, role, inc_cnt, d_err);
+        EMG_CUDA(cudaGetLastError());
+        if ((rc = check_err_flag(d_err, s))) return rc;
+    }
+    if (N > 0) {
+        k_check_roles<<<grid_for(N, T), T, 0, s>>>(role, N, inc_cnt, flag, d_err);
+        EMG_CUDA(cudaGetLastError());
+    }
+    if ((rc = scan_exclusive_i64(flag, flag_scan, N, scan_tmp, s))) return rc;
+    if ((rc = scan_exclusive_i64(inc_cnt, inc_ptr, N, scan_tmp, s))) return rc;
+    int64_t n_ent = 0;
+    EMG_CUDA(cudaMemcpyAsync(&n_ent, flag_scan + N, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    EMG_CUDA(cudaStreamSynchronize(s));
+    if ((rc = check_err_flag(d_err, s))) return rc;
+    if (n_ent > 0) {
+        k_compact<<<grid_for(N, T), T, 0, s>>>(flag_scan, inc_cnt, N, ent_list);
+        k_incidence_fill<<<grid_for(n_tets * 10, T), T, 0, s>>>(tet_to_field, n_tets, inc_ptr, cursor, inc);
+        k_incidence_sort<<<grid_for(n_ent, T), T, 0, s>>>(ent_list, n_ent, inc_ptr, inc);
+        k_pattern<<<grid_for(n_ent, kFillWarps, 152u * 32u), 32 * kFillWarps, 0, s>>>(
+            tet_to_field, n_tets, ent_list, n_ent, partner, inc_ptr, inc, 0, row_len, nullptr, nullptr, d_err);
+        EMG_CUDA(cudaGetLastError());
+    }
+    if ((rc = scan_exclusive_i64(row_len, indptr, N, scan_tmp, s))) return rc;
+    int64_t nnz = 0;
+    EMG_CUDA(cudaMemcpyAsync(&nnz, indptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    EMG_CUDA(cudaStreamSynchronize(s));
+    if ((rc = check_err_flag(d_err, s))) return rc;
+    *nnz_out = nnz;
+    if (nnz > indices_capacity || (nnz > 0 && indices == nullptr)) {
+        set_error("emg_csr_pattern_noalloc: indices capacity " + std::to_string(indices_capacity) +
+                  " is smaller than nnz " + std::to_string(nnz));
+        return EMG_ERR_LIMIT;
+    }
+    if (n_ent > 0) {
+        k_pattern<<<grid_for(n_ent, kFillWarps, 152u * 32u), 32 * kFillWarps, 0, s>>>(
+            tet_to_field, n_tets, ent_list, n_ent, partner, inc_ptr, inc, 1, nullptr, indptr, indices, d_err);
+        EMG_CUDA(cudaGetLastError());
+    }
+    return check_err_flag(d_err, s);
+}

@@ -80,6 +80,23 @@ int emg_assemble_tet_host(emg_plan* plan, const double* eps, const double* mu_in
 /* Releases the plan and its device memory. */
 void emg_plan_destroy(emg_plan* plan);
 
+/* CSR pattern without any device allocation.  No counterpart in the reference:
+ * an addition for callers that cannot call cudaMalloc, e.g. a host application
+ * that must not allocate device memory of its own (its memory is owned by
+ * another allocator, or cudaMalloc's implicit device synchronisation cannot be
+ * afforded in its loop).  Computes the same indptr/indices as emg_plan_create +
+ * emg_plan_pattern for meshes of at most 8192 tets and 65536 DOFs (larger sizes
+ * return EMG_ERR_LIMIT).  Inputs and outputs are caller-owned DEVICE arrays:
+ * tet_to_field (20, n_tets) int32, indptr (n_field+1) int64, indices
+ * (indices_capacity) int32; *nnz_out (host) receives nnz, and EMG_ERR_LIMIT is
+ * returned when nnz > indices_capacity.  The scratch is one ~4.9 MB device array
+ * in the library, held by every GPU that loads it until the process exits; the
+ * first call on a device looks up its address.  All calls share that array, so
+ * calls that overlap on the GPU (other streams or host threads) race.
+ * Synchronises ``stream``. */
+int emg_csr_pattern_noalloc(int64_t n_tets, int64_t n_field, const int32_t* tet_to_field, int64_t* indptr,
+                            int32_t* indices, int64_t indices_capacity, int64_t* nnz_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
