@@ -252,9 +252,9 @@ def run_gpu(args, rank, world):
         "e2e": {"value": e2e_val, "unit": "tets/s", "h2d_bytes_per_step": int(2 * 16 * nT),
                 "d2h_bytes_per_step": int(2 * 16 * nnz), "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "kernel": "k_fill",
+                     "peak_source": peak_kind, "kernel": "k_scales + k_fill_df (one assembly step)",
                      "algorithmic_bytes_per_launch": int(alg_bytes), "traffic": traffic_per_launch(n)},
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu:

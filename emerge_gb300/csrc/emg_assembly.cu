@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "emg_common.cuh"
+#include "emg_fill_df.cuh"
 
 namespace emg {
 namespace {
@@ -480,6 +481,7 @@ struct emg_plan {
     double* mu_dev = nullptr;
     double* E_dev = nullptr;
     double* B_dev = nullptr;
+    emg::DfPlan df;                // float-float fast fill (emg_fill_df.cu)
 };
 
 namespace {
@@ -487,6 +489,7 @@ namespace {
 void free_plan(emg_plan* p) {
     if (!p) return;
     emg::dfree(p->recs);
+    emg::df_plan_free(&p->df);
     emg::dfree(p->ent_list);
     emg::dfree(p->partner);
     emg::dfree(p->inc_ptr);
@@ -584,7 +587,6 @@ extern "C" int emg_plan_create(int64_t n_nodes, int64_t n_tets, int64_t n_edges,
     TRY(dalloc(&p->indptr, N + 1, "indptr"));
     TRY(dalloc(&scratch, scan_scratch_elems(N + 1) + 1, "scan scratch"));
     TRY(dalloc(&p->inc, n_tets * 10, "incidences"));
-    TRY(dalloc(&p->recs, n_tets, "tet records"));
     TRYC(cudaMemsetAsync(d_err, 0, sizeof(int), s));
     if (N > 0) {
         TRYC(cudaMemsetAsync(p->partner, 0xff, sizeof(int32_t) * N, s));
@@ -628,11 +630,19 @@ extern "C" int emg_plan_create(int64_t n_nodes, int64_t n_tets, int64_t n_edges,
         k_pattern<<<gp, 32 * kFillWarps, 0, s>>>(tet_to_field, n_tets, p->ent_list, p->n_ent, p->partner, p->inc_ptr,
                                                  p->inc, 1, nullptr, p->indptr, p->indices, d_err);
         TRYC(cudaGetLastError());
+    }
+    TRY(check_err_flag(d_err, s));
+    // fast fill: float-float blocks for entities within its limits
+    TRY(df_plan_build(nodes, n_nodes, tets, n_tets, edges, n_edges, tris, n_tris, tet_to_field, tet_to_edge,
+                      edge_lengths, p->ent_list, p->n_ent, p->inc_ptr, p->inc, p->indptr, &p->df, s));
+    // FP64 fill records only when some entity is outside the fast-fill limits
+    if (p->df.n_slow > 0) {
+        TRY(dalloc(&p->recs, n_tets, "tet records"));
         k_tet_prep<<<grid_for(n_tets, T), T, 0, s>>>(nodes, n_nodes, tets, n_tets, edges, n_edges, tris, n_tris,
                                                      tet_to_field, tet_to_edge, edge_lengths, p->recs, d_err);
         TRYC(cudaGetLastError());
+        TRY(check_err_flag(d_err, s));
     }
-    TRY(check_err_flag(d_err, s));
     dfree(d_err); dfree(role); dfree(cursor); dfree(inc_cnt); dfree(flag); dfree(flag_scan);
     dfree(row_len); dfree(scratch);
 #undef TRY
@@ -659,12 +669,16 @@ extern "C" int emg_assemble_tet(emg_plan* p, const double* eps, const double* mu
     EMG_CHECK_ARG(p->nnz == 0 || (eps && mu_inv && E_data && B_data), "emg_assemble_tet: NULL array");
     if (p->n_ent == 0) return EMG_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    const unsigned g = grid_for(p->n_ent, kFillWarps, 152u * 16u);
-    k_fill<<<g, 32 * kFillWarps, 0, s>>>(p->recs, p->ent_list, p->n_ent, p->partner, p->inc_ptr, p->inc, p->indptr,
-                                         p->indices, reinterpret_cast<const double2*>(eps),
-                                         reinterpret_cast<const double2*>(mu_inv), reinterpret_cast<double2*>(E_data),
-                                         reinterpret_cast<double2*>(B_data));
-    EMG_CUDA(cudaGetLastError());
+    int rc = df_fill(p->df, p->nT, p->partner, p->inc_ptr, p->inc, p->indptr, p->indices, eps, mu_inv, E_data, B_data, s);
+    if (rc) return rc;
+    if (p->df.n_slow > 0) {
+        const unsigned g = grid_for(p->df.n_slow, kFillWarps, 152u * 16u);
+        k_fill<<<g, 32 * kFillWarps, 0, s>>>(p->recs, p->df.slow, p->df.n_slow, p->partner, p->inc_ptr, p->inc,
+                                             p->indptr, p->indices, reinterpret_cast<const double2*>(eps),
+                                             reinterpret_cast<const double2*>(mu_inv),
+                                             reinterpret_cast<double2*>(E_data), reinterpret_cast<double2*>(B_data));
+        EMG_CUDA(cudaGetLastError());
+    }
     return EMG_OK;
 }
 

@@ -1,0 +1,630 @@
+// Float-float (pairs of FP32) assembly fill for GB300.
+//
+// GB300 executes FP64 at ~1/64 of its FP32 rate (1.2 vs 75 TFLOP/s measured),
+// so a straight FP64 element integration is compute-bound an order of magnitude
+// above the HBM floor of the write-once CSR fill.  This fill evaluates the
+// closed-form Nedelec-2 element blocks (fem/mth/tet.py:854-1088) in float-float
+// arithmetic (~48-bit significand, error-free products via FMA) on the FP32
+// pipes, accumulates each CSR entry in float-float in a fixed order, and
+// converts to FP64 with integer instructions when storing.  FP64 is used only
+// once per tet: for the geometry (plan) and the material scales (per fill).
+//
+// Work decomposition (entity-owner, as in emg_assembly.cu):
+//  * a warp owns one edge entity, or two face entities (rows r1/r2 each);
+//  * phase A computes the 2x2 blocks (row entity x edge column) of every
+//    incident tet, phase B the blocks with face columns; all lanes of a phase
+//    run the same block formula (no divergence), results staged in shared memory;
+//  * the owner phase: lane p sums, in ascending tet order, the staged entries
+//    that land on column position p of the entity's rows, scales them by the
+//    tet's complex material factors, and writes E and B once, coalesced.
+#include "emg_common.cuh"
+#include "emg_fill_df.cuh"
+#include "emg_geom.cuh"
+
+namespace emg {
+namespace dfk {
+
+struct df {
+    float h, l;
+};
+__device__ __forceinline__ df mk(float h, float l) {
+    df r;
+    r.h = h;
+    r.l = l;
+    return r;
+}
+// fast two-sum (|a| >= |b| or a == 0)
+__device__ __forceinline__ df fts(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return mk(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return mk(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ df operator+(df a, df b) {
+    const df s = two_sum(a.h, b.h);
+    return fts(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ df operator-(df a) { return mk(-a.h, -a.l); }
+__device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
+__device__ __forceinline__ df operator*(df a, df b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return fts(p, e);
+}
+__device__ __forceinline__ df operator*(df a, float c) {
+    const float p = __fmul_rn(a.h, c);
+    float e = __fmaf_rn(a.h, c, -p);
+    e = __fmaf_rn(a.l, c, e);
+    return fts(p, e);
+}
+__device__ __forceinline__ df operator*(float c, df a) { return a * c; }
+
+// hi + lo rounded (toward zero in the last bit) to FP64, with integer instructions.
+// Requires |lo| <= ulp(hi)/2 (every df op above renormalises).
+__device__ __forceinline__ double to_double(df a) {
+    const unsigned hb = __float_as_uint(a.h);
+    const unsigned eh = (hb >> 23) & 0xffu;
+    if (eh == 0u || eh == 0xffu) return (double)a.h + (double)a.l;   // zero, subnormal, inf, nan
+    const unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
+                                    ((unsigned long long)(eh + 896u) << 52) |
+                                    ((unsigned long long)(hb & 0x7fffffu) << 29);
+    const unsigned lb = __float_as_uint(a.l);
+    const unsigned el = (lb >> 23) & 0xffu;
+    if (el == 0u) return __longlong_as_double((long long)bits);
+    const long long m = (long long)((lb & 0x7fffffu) | 0x800000u);
+    const bool opp = ((lb ^ hb) & 0x80000000u) != 0u;
+    // position of lo's last mantissa bit in units of hi's FP64 ulp; one more when
+    // subtracting from an exact power of two (the result is in the lower binade)
+    int sh = (int)el - (int)eh + 29 + ((opp && (hb & 0x7fffffu) == 0u) ? 1 : 0);
+    const long long add = sh >= 0 ? (m << sh) : (sh > -40 ? (m >> -sh) : 0ll);
+    return __longlong_as_double((long long)(opp ? bits - (unsigned long long)add : bits + (unsigned long long)add));
+}
+
+__device__ __forceinline__ df split(double x) {
+    const float h = __double2float_rn(x);
+    return mk(h, __double2float_rn(x - (double)h));
+}
+
+// ---------------------------------------------------------------- records ---
+// Normalised tet invariants in float-float: G_p scaled by 2^-eG, lengths by 2^-eL.
+struct __align__(16) Rec2 {
+    float2 gram[10];    // G_p . G_q (p <= q)
+    float2 cdot[21];    // (G_a x G_b) . (G_c x G_d) over vertex pairs P <= R
+    float2 ds[6];       // vertex distances, pair order (0,1),(0,2),(0,3),(1,2),(1,3),(2,3)
+    float2 len[6];      // mesh edge lengths of edge slots
+    uint64_t lmap;      // packed local edge / face vertex maps (as TetRec::lmap)
+    int32_t dof[20];
+    int32_t pad[2];
+};
+static_assert(sizeof(Rec2) == 448, "Rec2 layout");
+
+__constant__ int8_t c_pidx[4][4] = {{-1, 0, 1, 2}, {0, -1, 3, 4}, {1, 3, -1, 5}, {2, 4, 5, -1}};
+__constant__ int8_t c_gidx[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+// simplex monomial integrals x 7! (exact small integers), letters 0..4, 0 = absent
+__constant__ float c_vint[625];
+
+__device__ __forceinline__ int cidx(int P, int R) {
+    if (P > R) { const int t = P; P = R; R = t; }
+    return P * 6 - (P * (P - 1)) / 2 + (R - P);
+}
+
+// Thread per tet (plan time, FP64): invariants normalised by powers of two and
+// the FP64 scales that undo the normalisation, the 1/(6V)^k factors and the 7!.
+__global__ void k_prep2(const double* __restrict__ nodes, int64_t nN, const int32_t* __restrict__ tets, int64_t nT,
+                        const int32_t* __restrict__ edges, int64_t nE, const int32_t* __restrict__ tris, int64_t nTri,
+                        const int32_t* __restrict__ t2f, const int32_t* __restrict__ t2e,
+                        const double* __restrict__ edge_len, Rec2* __restrict__ recs, double2* __restrict__ gscale,
+                        int* err) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nT; t += (int64_t)gridDim.x * blockDim.x) {
+        int32_t vid[4];
+        double x[4], y[4], z[4];
+        for (int k = 0; k < 4; ++k) {
+            vid[k] = tets[k * nT + t];
+            x[k] = nodes[vid[k]];
+            y[k] = nodes[nN + vid[k]];
+            z[k] = nodes[2 * nN + vid[k]];
+        }
+        double G[4][3], V;
+        geom::tet_bcd(x, y, z, G, &V);
+        double gmax = 0.0;
+        for (int i = 0; i < 4; ++i)
+            for (int c = 0; c < 3; ++c) gmax = fmax(gmax, fabs(G[i][c]));
+        const int eG = gmax > 0.0 ? ilogb(gmax) : 0;
+        for (int i = 0; i < 4; ++i)
+            for (int c = 0; c < 3; ++c) G[i][c] = scalbn(G[i][c], -eG);
+        Rec2 r;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p; q < 4; ++q) {
+                const df v = split(G[p][0] * G[q][0] + G[p][1] * G[q][1] + G[p][2] * G[q][2]);
+                r.gram[c_gidx[p][q]] = make_float2(v.h, v.l);
+            }
+        const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
+        double X[6][3], dsv[6], lenv[6];
+        double lmax = 0.0;
+        for (int P = 0; P < 6; ++P) {
+            const double* u = G[pa[P]];
+            const double* v = G[pb[P]];
+            X[P][0] = u[1] * v[2] - u[2] * v[1];
+            X[P][1] = u[2] * v[0] - u[0] * v[2];
+            X[P][2] = u[0] * v[1] - u[1] * v[0];
+            const double dx = x[pa[P]] - x[pb[P]], dy = y[pa[P]] - y[pb[P]], dz = z[pa[P]] - z[pb[P]];
+            dsv[P] = sqrt(dx * dx + dy * dy + dz * dz);
+            lmax = fmax(lmax, dsv[P]);
+        }
+        for (int P = 0; P < 6; ++P)
+            for (int R = P; R < 6; ++R) {
+                const df v = split(X[P][0] * X[R][0] + X[P][1] * X[R][1] + X[P][2] * X[R][2]);
+                r.cdot[cidx(P, R)] = make_float2(v.h, v.l);
+            }
+        uint64_t lm = 0;
+        bool ok = true;
+        for (int e = 0; e < 6; ++e) {
+            lenv[e] = edge_len[t2e[e * nT + t]];
+            lmax = fmax(lmax, lenv[e]);
+            const int32_t eid = t2f[e * nT + t];
+            if (eid < 0 || eid >= nE) { ok = false; continue; }
+            for (int j = 0; j < 2; ++j) {
+                const int32_t g = edges[j * nE + eid];
+                int loc = -1;
+                for (int k = 0; k < 4; ++k) if (vid[k] == g) { loc = k; break; }
+                if (loc < 0) { ok = false; loc = 0; }
+                lm |= (uint64_t)loc << (4 * e + 2 * j);
+            }
+        }
+        for (int f = 0; f < 4; ++f) {
+            const int64_t tri = (int64_t)t2f[(6 + f) * nT + t] - nE;
+            if (tri < 0 || tri >= nTri) { ok = false; continue; }
+            for (int j = 0; j < 3; ++j) {
+                const int32_t g = tris[j * nTri + tri];
+                int loc = -1;
+                for (int k = 0; k < 4; ++k) if (vid[k] == g) { loc = k; break; }
+                if (loc < 0) { ok = false; loc = 0; }
+                lm |= (uint64_t)loc << (24 + 6 * f + 2 * j);
+            }
+        }
+        if (!ok) atomicOr(err, 1);
+        const int eL = lmax > 0.0 ? ilogb(lmax) : 0;
+        for (int P = 0; P < 6; ++P) {
+            const df a = split(scalbn(dsv[P], -eL));
+            const df b = split(scalbn(lenv[P], -eL));
+            r.ds[P] = make_float2(a.h, a.l);
+            r.len[P] = make_float2(b.h, b.l);
+        }
+        r.lmap = lm;
+        for (int k = 0; k < 20; ++k) r.dof[k] = t2f[k * nT + t];
+        r.pad[0] = r.pad[1] = 0;
+        recs[t] = r;
+        const double V6 = 6.0 * V;
+        const double V6sq = V6 * V6;
+        const double kd = V6 * (1.0 / (V6sq * V6sq));
+        const double kf = V6 * (1.0 / V6sq);
+        // D entries scale as len^2 G^4, F entries as len^2 G^2; the integers carry 7!
+        gscale[t] = make_double2(scalbn(kd, 4 * eG + 2 * eL) / 5040.0, scalbn(kf, 2 * eG + 2 * eL) / 5040.0);
+    }
+}
+
+// Per fill (FP64, thread per tet): complex scales sE = mu_inv * gscale.x and
+// sB = eps * gscale.y, stored as float-float (re.h, re.l, im.h, im.l).
+__global__ void k_scales(const double2* __restrict__ gscale, const double2* __restrict__ eps,
+                         const double2* __restrict__ mu_inv, int64_t nT, float4* __restrict__ tscale) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nT; t += (int64_t)gridDim.x * blockDim.x) {
+        const double2 g = gscale[t], m = mu_inv[t], e = eps[t];
+        const df a = split(m.x * g.x), b = split(m.y * g.x), c = split(e.x * g.y), d = split(e.y * g.y);
+        tscale[2 * t] = make_float4(a.h, a.l, b.h, b.l);
+        tscale[2 * t + 1] = make_float4(c.h, c.l, d.h, d.l);
+    }
+}
+
+// ------------------------------------------------------------- the blocks ---
+struct Tet {
+    const Rec2* r;
+    __device__ __forceinline__ df g(int p, int q) const {
+        const float2 v = r->gram[c_gidx[p][q]];
+        return mk(v.x, v.y);
+    }
+    __device__ __forceinline__ df cc(int p, int q, int s1, int s2) const {
+        if (p == q || s1 == s2) return mk(0.f, 0.f);
+        const float2 v = r->cdot[cidx(c_pidx[p][q], c_pidx[s1][s2])];
+        return ((p < q) == (s1 < s2)) ? mk(v.x, v.y) : mk(-v.x, -v.y);
+    }
+    __device__ __forceinline__ df ds(int p, int q) const {
+        const float2 v = r->ds[c_pidx[p][q]];
+        return mk(v.x, v.y);
+    }
+    __device__ __forceinline__ df len(int e) const {
+        const float2 v = r->len[e];
+        return mk(v.x, v.y);
+    }
+};
+
+__device__ __forceinline__ float v4(const float* vt, int a, int b, int c, int d) {
+    return vt[(((a + 1) * 5 + (b + 1)) * 5 + (c + 1)) * 5 + (d + 1)];
+}
+__device__ __forceinline__ float v2(const float* vt, int a, int b) { return vt[((a + 1) * 5 + (b + 1)) * 25]; }
+__device__ __forceinline__ void ev(uint64_t m, int e, int& a, int& b) {
+    a = (int)((m >> (4 * e)) & 3);
+    b = (int)((m >> (4 * e + 2)) & 3);
+}
+__device__ __forceinline__ void fv(uint64_t m, int f, int& a, int& b, int& c) {
+    a = (int)((m >> (24 + 6 * f)) & 3);
+    b = (int)((m >> (24 + 6 * f + 2)) & 3);
+    c = (int)((m >> (24 + 6 * f + 4)) & 3);
+}
+
+// Block outputs: D[a][b], F[a][b] (row mode a, column mode b), as in emg_assembly.cu.
+__device__ void blk_ee(const Tet& T, const float* vt, uint64_t lm, int e, int j, df D[2][2], df F[2][2]) {
+    int A, B, C, Dl;
+    ev(lm, e, A, B);
+    ev(lm, j, C, Dl);
+    const df Q2 = T.len(e) * T.len(j);
+    const df Q = (Q2 * T.cc(A, B, C, Dl)) * 9.0f;
+    D[0][0] = Q * v2(vt, A, C);
+    D[0][1] = Q * v2(vt, A, Dl);
+    D[1][0] = Q * v2(vt, B, C);
+    D[1][1] = Q * v2(vt, B, Dl);
+    const df gAC = T.g(A, C), gAD = T.g(A, Dl), gBC = T.g(B, C), gBD = T.g(B, Dl);
+    F[0][0] = Q2 * (gAC * v4(vt, A, B, C, Dl) - gAD * v4(vt, A, B, C, C) - gBC * v4(vt, A, A, C, Dl) + gBD * v4(vt, A, A, C, C));
+    F[0][1] = Q2 * (gAC * v4(vt, A, B, Dl, Dl) - gAD * v4(vt, A, B, C, Dl) - gBC * v4(vt, A, A, Dl, Dl) + gBD * v4(vt, A, A, C, Dl));
+    F[1][0] = Q2 * (gAC * v4(vt, B, B, C, Dl) - gAD * v4(vt, B, B, C, C) - gBC * v4(vt, A, B, C, Dl) + gBD * v4(vt, A, B, C, C));
+    F[1][1] = Q2 * (gAC * v4(vt, B, B, Dl, Dl) - gAD * v4(vt, B, B, C, Dl) - gBC * v4(vt, A, B, Dl, Dl) + gBD * v4(vt, A, B, C, Dl));
+}
+
+__device__ void blk_ef(const Tet& T, const float* vt, uint64_t lm, int e, int f, df D[2][2], df F[2][2]) {
+    int A, B, C, Dl, Fl;
+    ev(lm, e, A, B);
+    fv(lm, f, C, Dl, Fl);
+    const df L1 = T.len(e);
+    const df c0 = L1 * T.ds(C, Fl), c1 = L1 * T.ds(C, Dl);
+    const df AI = T.cc(A, B, C, Fl), AJ = T.cc(A, B, Dl, Fl), AK = T.cc(A, B, C, Dl);
+    D[0][0] = c0 * (AI * (-6.0f * v2(vt, A, Dl)) - AJ * (3.0f * v2(vt, A, C)) - AK * (3.0f * v2(vt, A, Fl)));
+    D[0][1] = c1 * (AK * (6.0f * v2(vt, A, Fl)) + AI * (3.0f * v2(vt, A, Dl)) - AJ * (3.0f * v2(vt, A, C)));
+    D[1][0] = c0 * (AI * (-6.0f * v2(vt, B, Dl)) - AJ * (3.0f * v2(vt, B, C)) - AK * (3.0f * v2(vt, B, Fl)));
+    D[1][1] = c1 * (AK * (6.0f * v2(vt, B, Fl)) + AI * (3.0f * v2(vt, B, Dl)) - AJ * (3.0f * v2(vt, B, C)));
+    const df gAF = T.g(A, Fl), gAC = T.g(A, C), gBF = T.g(B, Fl), gBC = T.g(B, C), gAD = T.g(A, Dl), gBD = T.g(B, Dl);
+    F[0][0] = c0 * (gAF * v4(vt, A, B, C, Dl) - gAC * v4(vt, A, B, Dl, Fl) - gBF * v4(vt, A, A, C, Dl) + gBC * v4(vt, A, A, Dl, Fl));
+    F[0][1] = c1 * (gAC * v4(vt, A, B, Dl, Fl) - gAD * v4(vt, A, B, Fl, C) - gBC * v4(vt, A, A, Dl, Fl) + gBD * v4(vt, A, A, C, Fl));
+    F[1][0] = c0 * (gAF * v4(vt, B, B, C, Dl) - gAC * v4(vt, B, B, Dl, Fl) - gBF * v4(vt, A, B, C, Dl) + gBC * v4(vt, A, B, Dl, Fl));
+    F[1][1] = c1 * (gAC * v4(vt, B, B, Dl, Fl) - gAD * v4(vt, B, B, Fl, C) - gBC * v4(vt, A, B, Dl, Fl) + gBD * v4(vt, A, B, Fl, C));
+}
+
+__device__ void blk_ff(const Tet& T, const float* vt, uint64_t lm, int fi, int fj, df D[2][2], df F[2][2]) {
+    int A, B, E, C, Dl, Fl;
+    fv(lm, fi, A, B, E);
+    fv(lm, fj, C, Dl, Fl);
+    const df Lac1 = T.ds(A, E), Lab1 = T.ds(A, B), Lac2 = T.ds(C, Fl), Lab2 = T.ds(C, Dl);
+    const df AK = T.cc(A, E, C, Fl), AL = T.cc(A, E, Dl, Fl), AM = T.cc(A, E, C, Dl);
+    const df AN = T.cc(B, E, C, Fl), AO = T.cc(B, E, Dl, Fl), AP = T.cc(B, E, C, Dl);
+    const df AQ = T.cc(A, B, C, Fl), AR = T.cc(A, B, Dl, Fl), AS = T.cc(A, B, C, Dl);
+    const float vAD = v2(vt, A, Dl), vAC = v2(vt, A, C), vAF = v2(vt, A, Fl);
+    const float vBF = v2(vt, B, Fl), vBC = v2(vt, B, C), vBD = v2(vt, B, Dl);
+    const float vDE = v2(vt, E, Dl), vEF = v2(vt, E, Fl), vCE = v2(vt, E, C);
+    const df Q1 = AN * (2.0f * vAD) + AO * vAC + AP * vAF;
+    const df Q2 = AO * vAC - AP * (2.0f * vAF) - AN * vAD;
+    D[0][0] = (Lac1 * Lac2) * (AK * (4.0f * vBD) + AL * (2.0f * vBC) + AM * (2.0f * vBF) + Q1 + AQ * (2.0f * vDE) + AR * vCE + AS * vEF);
+    D[0][1] = (Lac1 * Lab2) * (AL * (2.0f * vBC) - AM * (4.0f * vBF) - AK * (2.0f * vBD) + Q2 - AS * (2.0f * vEF) - AQ * vDE + AR * vCE);
+    D[1][0] = (Lab1 * Lac2) * (Q1 - AQ * (4.0f * vDE) - AR * (2.0f * vCE) - AS * (2.0f * vEF) - AK * (2.0f * vBD) - AL * vBC - AM * vBF);
+    D[1][1] = (Lab1 * Lab2) * (AS * (4.0f * vEF) + AQ * (2.0f * vDE) - AR * (2.0f * vCE) + AM * (2.0f * vBF) + AK * vBD - AL * vBC + Q2);
+    const df gEF = T.g(E, Fl), gEC = T.g(E, C), gAF = T.g(A, Fl), gAC = T.g(A, C), gED = T.g(E, Dl);
+    const df gAD = T.g(A, Dl), gBF = T.g(B, Fl), gBC = T.g(B, C), gBD = T.g(B, Dl);
+    const float vABCD = v4(vt, A, B, C, Dl), vABDF = v4(vt, A, B, Dl, Fl), vACEF = v4(vt, A, C, E, Fl);
+    const float vABCF = v4(vt, A, B, Fl, C), vBCDX = v4(vt, B, C, Dl, Fl), vBDEF = v4(vt, B, E, Dl, Fl);
+    const float vACDE = v4(vt, E, A, C, Dl), vBCEF = v4(vt, B, E, Fl, C), vADEF = v4(vt, E, A, Dl, Fl);
+    F[0][0] = (Lac1 * Lac2) * (gEF * vABCD - gEC * vABDF - gAF * vBCDX + gAC * vBDEF);
+    F[0][1] = (Lac1 * Lab2) * (gEC * vABDF - gED * vABCF - gAC * vBDEF + gAD * vBCEF);
+    F[1][0] = (Lab1 * Lac2) * (gAF * vBCDX - gAC * vBDEF - gBF * vACDE + gBC * vADEF);
+    F[1][1] = (Lab1 * Lab2) * (gAC * vBDEF - gAD * vBCEF - gBC * vADEF + gBD * vACEF);
+}
+
+// ----------------------------------------------------------------- fill ---
+constexpr int kWarps = 4;
+constexpr int kKmax = kDfMaxInc;        // incidences per warp group
+constexpr int kNmax = kDfMaxCols;       // columns per entity
+
+struct __align__(16) WarpSm {
+    float4 stage[kKmax * 10][4];        // per item: D (4 df) then F (4 df)
+    float4 sc[kKmax][2];                // per incidence: sE, sB (re.h, re.l, im.h, im.l)
+    int32_t cols[2][kNmax];
+    int32_t tet[kKmax];
+    int8_t slot[kKmax];
+    uint8_t tab[kKmax][kNmax];          // (column slot j | column mode << 4) or 0xff
+};
+
+__device__ __forceinline__ int find_col(const int32_t* cols, int n, int32_t c) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cols[mid] < c) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void store_df(float4* dst, const df X[2][2]) {
+    dst[0] = make_float4(X[0][0].h, X[0][0].l, X[0][1].h, X[0][1].l);
+    dst[1] = make_float4(X[1][0].h, X[1][0].l, X[1][1].h, X[1][1].l);
+}
+
+__global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict__ recs, const int32_t* __restrict__ groups,
+                                                         int64_t n_groups, const int32_t* __restrict__ partner,
+                                                         const int64_t* __restrict__ inc_ptr, const int64_t* __restrict__ inc,
+                                                         const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                                         const float4* __restrict__ tscale, double2* __restrict__ E,
+                                                         double2* __restrict__ B) {
+    __shared__ float vt[625];
+    __shared__ WarpSm sm_all[kWarps];
+    for (int i = threadIdx.x; i < 625; i += blockDim.x) vt[i] = c_vint[i];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    WarpSm& sm = sm_all[w];
+    for (int64_t g = blockIdx.x * (int64_t)kWarps + w; g < n_groups; g += (int64_t)gridDim.x * kWarps) {
+        const int32_t ent[2] = {groups[2 * g], groups[2 * g + 1]};
+        const int nsub = ent[1] >= 0 ? 2 : 1;
+        int64_t b1[2], b2[2], i0[2];
+        int n[2], k[2], kofs[2];
+        int ktot = 0;
+        for (int u = 0; u < nsub; ++u) {
+            const int32_t r1 = ent[u];
+            b1[u] = indptr[r1];
+            b2[u] = indptr[partner[r1]];
+            n[u] = (int)(indptr[r1 + 1] - b1[u]);
+            i0[u] = inc_ptr[r1];
+            k[u] = (int)(inc_ptr[r1 + 1] - i0[u]);
+            kofs[u] = ktot;
+            ktot += k[u];
+        }
+        for (int u = 0; u < nsub; ++u)
+            for (int c = lane; c < n[u]; c += 32) sm.cols[u][c] = __ldg(indices + b1[u] + c);
+        for (int q = lane; q < ktot; q += 32) {
+            const int u = (nsub == 2 && q >= kofs[1]) ? 1 : 0;
+            const int64_t code = inc[i0[u] + (q - kofs[u])];
+            const int64_t t = code >> 4;
+            sm.tet[q] = (int32_t)t;
+            sm.slot[q] = (int8_t)(code & 15);
+            sm.sc[q][0] = __ldg(tscale + 2 * t);
+            sm.sc[q][1] = __ldg(tscale + 2 * t + 1);
+        }
+        for (int u = 0; u < nsub; ++u)
+            for (int q = 0; q < k[u]; ++q)
+                for (int c = lane; c < n[u]; c += 32) sm.tab[kofs[u] + q][c] = 0xff;
+        __syncwarp();
+        // phase A: edge columns (j = 0..5); phase B: face columns (j = 6..9)
+        for (int ph = 0; ph < 2; ++ph) {
+            const int per = ph == 0 ? 6 : 4;
+            const int nitems = ktot * per;
+            for (int a = lane; a < nitems; a += 32) {
+                const int q = a / per;
+                const int j = (ph == 0 ? 0 : 6) + a % per;
+                const int s = sm.slot[q];
+                const Rec2* rp = recs + sm.tet[q];
+                const Tet T{rp};
+                const uint64_t lm = rp->lmap;
+                df D[2][2], F[2][2];
+                if (s < 6) {
+                    if (j < 6) blk_ee(T, vt, lm, s, j, D, F);
+                    else blk_ef(T, vt, lm, s, j - 6, D, F);
+                } else if (j < 6) {
+                    df Dt[2][2], Ft[2][2];
+                    blk_ef(T, vt, lm, j, s - 6, Dt, Ft);
+                    D[0][0] = Dt[0][0]; D[0][1] = Dt[1][0]; D[1][0] = Dt[0][1]; D[1][1] = Dt[1][1];
+                    F[0][0] = Ft[0][0]; F[0][1] = Ft[1][0]; F[1][0] = Ft[0][1]; F[1][1] = Ft[1][1];
+                } else {
+                    blk_ff(T, vt, lm, s - 6, j - 6, D, F);
+                }
+                float4* st = sm.stage[q * 10 + j];
+                store_df(st, D);
+                store_df(st + 2, F);
+                const int u = (nsub == 2 && q >= kofs[1]) ? 1 : 0;
+                const int p1 = find_col(sm.cols[u], n[u], __ldg(&rp->dof[j]));
+                const int p2 = find_col(sm.cols[u], n[u], __ldg(&rp->dof[j + 10]));
+                sm.tab[q][p1] = (uint8_t)j;
+                sm.tab[q][p2] = (uint8_t)(j | 16);
+            }
+        }
+        __syncwarp();
+        // owner phase
+        for (int u = 0; u < nsub; ++u) {
+            bool e_real = true;
+            for (int q = kofs[u]; q < kofs[u] + k[u]; ++q) e_real &= (sm.sc[q][0].z == 0.f && sm.sc[q][0].w == 0.f);
+            for (int p = lane; p < n[u]; p += 32) {
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    df er = mk(0.f, 0.f), ei = mk(0.f, 0.f), br = mk(0.f, 0.f), bi = mk(0.f, 0.f);
+                    for (int q = kofs[u]; q < kofs[u] + k[u]; ++q) {
+                        const uint8_t x = sm.tab[q][p];
+                        if (x == 0xff) continue;
+                        const int j = x & 15, b = x >> 4;
+                        const float4* st = sm.stage[q * 10 + j];
+                        const float4 dv = st[a];
+                        const float4 fvv = st[2 + a];
+                        const df Dv = b ? mk(dv.z, dv.w) : mk(dv.x, dv.y);
+                        const df Fv = b ? mk(fvv.z, fvv.w) : mk(fvv.x, fvv.y);
+                        const float4 se = sm.sc[q][0], sb = sm.sc[q][1];
+                        er = er + mk(se.x, se.y) * Dv;
+                        if (!e_real) ei = ei + mk(se.z, se.w) * Dv;
+                        br = br + mk(sb.x, sb.y) * Fv;
+                        bi = bi + mk(sb.z, sb.w) * Fv;
+                    }
+                    const int64_t o = (a == 0 ? b1[u] : b2[u]) + p;
+                    E[o] = make_double2(to_double(er), e_real ? 0.0 : to_double(ei));
+                    B[o] = make_double2(to_double(br), to_double(bi));
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------- plan-time grouping ---
+// Classify entities: fast edges (k <= kKmax, n <= kNmax), fast faces (pairs),
+// everything else to the FP64 fallback list.
+__global__ void k_classify(const int32_t* __restrict__ ent_list, int64_t n_ent, const int64_t* __restrict__ inc_ptr,
+                           const int64_t* __restrict__ inc, const int64_t* __restrict__ indptr, int64_t* fe,
+                           int64_t* ff, int64_t* fs) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_ent; e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = ent_list[e];
+        const int64_t k = inc_ptr[r + 1] - inc_ptr[r];
+        const int64_t n = indptr[r + 1] - indptr[r];
+        int kind = -1;   // 0 edge, 1 face
+        bool uniform = true;
+        for (int64_t i = inc_ptr[r]; i < inc_ptr[r + 1]; ++i) {
+            const int kk = ((inc[i] & 15) < 6) ? 0 : 1;
+            if (kind < 0) kind = kk;
+            uniform &= (kk == kind);
+        }
+        const bool fits = uniform && n <= kNmax && ((kind == 0 && k <= kKmax) || (kind == 1 && k <= kKmax / 2));
+        fe[e] = (fits && kind == 0) ? 1 : 0;
+        ff[e] = (fits && kind == 1) ? 1 : 0;
+        fs[e] = fits ? 0 : 1;
+    }
+}
+
+__global__ void k_groups(const int32_t* __restrict__ ent_list, int64_t n_ent, const int64_t* fe, const int64_t* fe_scan,
+                         const int64_t* ff, const int64_t* ff_scan, const int64_t* fs, const int64_t* fs_scan,
+                         int64_t n_fe, int32_t* groups, int32_t* slow) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_ent; e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = ent_list[e];
+        if (fe[e]) {
+            const int64_t g = fe_scan[e];
+            groups[2 * g] = r;
+            groups[2 * g + 1] = -1;
+        } else if (ff[e]) {
+            const int64_t f = ff_scan[e];
+            groups[2 * (n_fe + f / 2) + (f & 1)] = r;
+        } else {
+            slow[fs_scan[e]] = r;
+        }
+    }
+}
+
+}  // namespace dfk
+
+// ------------------------------------------------------------------ host ---
+namespace {
+bool g_vint_ready[64] = {false};
+
+int upload_vint() {
+    int dev = 0;
+    EMG_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && g_vint_ready[dev]) return EMG_OK;
+    static const double fact[10] = {1, 1, 2, 6, 24, 120, 720, 5040, 40320, 362880};
+    float h[625];
+    for (int a = 0; a < 5; ++a)
+        for (int b = 0; b < 5; ++b)
+            for (int c = 0; c < 5; ++c)
+                for (int d = 0; d < 5; ++d) {
+                    int k[5] = {0, 0, 0, 0, 0};
+                    k[a]++; k[b]++; k[c]++; k[d]++;
+                    const double num = fact[k[1]] * fact[k[2]] * fact[k[3]] * fact[k[4]];
+                    h[((a * 5 + b) * 5 + c) * 5 + d] = (float)(5040.0 * num / fact[k[1] + k[2] + k[3] + k[4] + 3]);
+                }
+    EMG_CUDA(cudaMemcpyToSymbol(dfk::c_vint, h, sizeof(h)));
+    if (dev >= 0 && dev < 64) g_vint_ready[dev] = true;
+    return EMG_OK;
+}
+}  // namespace
+
+void df_plan_free(DfPlan* p) {
+    dfree(p->recs);
+    dfree(p->gscale);
+    dfree(p->tscale);
+    dfree(p->groups);
+    dfree(p->slow);
+    p->n_groups = p->n_slow = 0;
+}
+
+int df_plan_build(const double* nodes, int64_t nN, const int32_t* tets, int64_t nT, const int32_t* edges, int64_t nE,
+                  const int32_t* tris, int64_t nTri, const int32_t* t2f, const int32_t* t2e, const double* edge_len,
+                  const int32_t* ent_list, int64_t n_ent, const int64_t* inc_ptr, const int64_t* inc,
+                  const int64_t* indptr, DfPlan* p, cudaStream_t s) {
+    int rc = upload_vint();
+    if (rc) return rc;
+    *p = DfPlan();
+    int* d_err = nullptr;
+    int64_t *fe = nullptr, *ff = nullptr, *fs = nullptr, *fe_s = nullptr, *ff_s = nullptr, *fs_s = nullptr, *tmp = nullptr;
+    auto cleanup = [&]() {
+        dfree(d_err); dfree(fe); dfree(ff); dfree(fs); dfree(fe_s); dfree(ff_s); dfree(fs_s); dfree(tmp);
+    };
+#define TRY(x) do { int _r = (x); if (_r) { cleanup(); df_plan_free(p); return _r; } } while (0)
+    TRY(dalloc(&d_err, 1, "df err"));
+    TRY(dalloc(reinterpret_cast<dfk::Rec2**>(&p->recs), nT, "df records"));
+    TRY(dalloc(&p->gscale, nT, "df geometric scales"));
+    TRY(dalloc(&p->tscale, 2 * nT, "df material scales"));
+    {
+        const cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), s);
+        if (e != cudaSuccess) TRY(cuda_status(e, "memset"));
+    }
+    const int T = 256;
+    if (nT > 0) {
+        dfk::k_prep2<<<grid_for(nT, T), T, 0, s>>>(nodes, nN, tets, nT, edges, nE, tris, nTri, t2f, t2e, edge_len,
+                                                   reinterpret_cast<dfk::Rec2*>(p->recs), p->gscale, d_err);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) TRY(cuda_status(e, "k_prep2"));
+    }
+    TRY(dalloc(&fe, n_ent + 1, "fe"));
+    TRY(dalloc(&ff, n_ent + 1, "ff"));
+    TRY(dalloc(&fs, n_ent + 1, "fs"));
+    TRY(dalloc(&fe_s, n_ent + 1, "fe scan"));
+    TRY(dalloc(&ff_s, n_ent + 1, "ff scan"));
+    TRY(dalloc(&fs_s, n_ent + 1, "fs scan"));
+    TRY(dalloc(&tmp, scan_scratch_elems(n_ent + 1) + 1, "scan tmp"));
+    if (n_ent > 0) {
+        dfk::k_classify<<<grid_for(n_ent, T), T, 0, s>>>(ent_list, n_ent, inc_ptr, inc, indptr, fe, ff, fs);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) TRY(cuda_status(e, "k_classify"));
+    }
+    TRY(scan_exclusive_i64(fe, fe_s, n_ent, tmp, s));
+    TRY(scan_exclusive_i64(ff, ff_s, n_ent, tmp, s));
+    TRY(scan_exclusive_i64(fs, fs_s, n_ent, tmp, s));
+    int64_t cnt[3] = {0, 0, 0};
+    int h_err = 0;
+    if (cudaMemcpyAsync(&cnt[0], fe_s + n_ent, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&cnt[1], ff_s + n_ent, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&cnt[2], fs_s + n_ent, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        TRY(cuda_status(cudaGetLastError(), "df plan readback"));
+    if (h_err) {
+        set_error("mesh check failed: an edge/face vertex is not a vertex of its tet");
+        TRY(EMG_ERR_MESH);
+    }
+    p->n_groups = cnt[0] + (cnt[1] + 1) / 2;
+    p->n_slow = cnt[2];
+    TRY(dalloc(&p->groups, 2 * p->n_groups + 2, "df groups"));
+    TRY(dalloc(&p->slow, p->n_slow + 1, "df slow list"));
+    if (p->n_groups > 0 && cudaMemsetAsync(p->groups, 0xff, sizeof(int32_t) * (2 * p->n_groups + 2), s) != cudaSuccess)
+        TRY(cuda_status(cudaGetLastError(), "memset groups"));
+    if (n_ent > 0) {
+        dfk::k_groups<<<grid_for(n_ent, T), T, 0, s>>>(ent_list, n_ent, fe, fe_s, ff, ff_s, fs, fs_s, cnt[0], p->groups,
+                                                        p->slow);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) TRY(cuda_status(e, "k_groups"));
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess) TRY(cuda_status(cudaGetLastError(), "df plan sync"));
+#undef TRY
+    cleanup();
+    return EMG_OK;
+}
+
+int df_fill(const DfPlan& p, int64_t nT, const int32_t* partner, const int64_t* inc_ptr, const int64_t* inc,
+            const int64_t* indptr, const int32_t* indices, const double* eps, const double* mu_inv, double* E,
+            double* B, cudaStream_t s) {
+    if (nT > 0) {
+        dfk::k_scales<<<grid_for(nT, 256), 256, 0, s>>>(p.gscale, reinterpret_cast<const double2*>(eps),
+                                                         reinterpret_cast<const double2*>(mu_inv), nT, p.tscale);
+        EMG_CUDA(cudaGetLastError());
+    }
+    if (p.n_groups > 0) {
+        const unsigned g = grid_for(p.n_groups, dfk::kWarps, 152u * 32u);
+        dfk::k_fill_df<<<g, 32 * dfk::kWarps, 0, s>>>(reinterpret_cast<const dfk::Rec2*>(p.recs), p.groups, p.n_groups,
+                                                       partner, inc_ptr, inc, indptr, indices, p.tscale,
+                                                       reinterpret_cast<double2*>(E), reinterpret_cast<double2*>(B));
+        EMG_CUDA(cudaGetLastError());
+    }
+    return EMG_OK;
+}
+
+}  // namespace emg

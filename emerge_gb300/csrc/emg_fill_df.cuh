@@ -1,0 +1,34 @@
+// Float-float fill of the tet assembly (emg_fill_df.cu): plan-side data and entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace emg {
+
+constexpr int kDfMaxInc = 12;    // incident tets per edge entity handled by the fast fill
+constexpr int kDfMaxCols = 128;  // CSR columns per entity handled by the fast fill
+
+// Device arrays of the fast fill, owned by the assembly plan.
+struct DfPlan {
+    void* recs = nullptr;        // per-tet normalised float-float invariants (448 B/tet)
+    double2* gscale = nullptr;   // per-tet FP64 scales of the curl-curl and mass blocks
+    float4* tscale = nullptr;    // per-tet complex material scales (written by each fill)
+    int32_t* groups = nullptr;   // warp work units: (edge entity, -1) or (face entity, face entity | -1)
+    int32_t* slow = nullptr;     // entities outside the fast-fill limits (FP64 fill)
+    int64_t n_groups = 0;
+    int64_t n_slow = 0;
+};
+
+int df_plan_build(const double* nodes, int64_t nN, const int32_t* tets, int64_t nT, const int32_t* edges, int64_t nE,
+                  const int32_t* tris, int64_t nTri, const int32_t* t2f, const int32_t* t2e, const double* edge_len,
+                  const int32_t* ent_list, int64_t n_ent, const int64_t* inc_ptr, const int64_t* inc,
+                  const int64_t* indptr, DfPlan* p, cudaStream_t s);
+
+int df_fill(const DfPlan& p, int64_t nT, const int32_t* partner, const int64_t* inc_ptr, const int64_t* inc,
+            const int64_t* indptr, const int32_t* indices, const double* eps, const double* mu_inv, double* E,
+            double* B, cudaStream_t s);
+
+void df_plan_free(DfPlan* p);
+
+}  // namespace emg

@@ -133,3 +133,21 @@ def test_anisotropic_material_is_rejected(torch_cuda):
     er[0, 1, 0] = 0.1
     with pytest.raises(NotImplementedError):
         tet_mass_stiffness_matrices(field, er, z["ur_a"])
+
+
+def test_high_valence_edge_matches_oracle(torch_cuda):
+    """An edge shared by 16 tets (beyond the float-float fill's 12) takes the FP64 fill."""
+    from emerge_gb300.assembly import AssemblyPlan, tet_mass_stiffness_matrices
+    from emerge_gb300.mesh import Nedelec2Basis, TetMesh
+    M = 16
+    ang = 2 * np.pi * np.arange(M) / M
+    ring = np.stack([np.cos(ang), np.sin(ang), 0.5 + 0.1 * np.sin(3 * ang)]) * 1e-3
+    nodes = np.concatenate([np.array([[0, 0], [0, 0], [0, 1e-3]]), ring], axis=1)
+    tets = np.stack([np.zeros(M, int), np.ones(M, int), 2 + np.arange(M), 2 + (np.arange(M) + 1) % M])
+    m = TetMesh(nodes, tets)
+    field = Nedelec2Basis(m)
+    er, ur = _random_materials(M, 11, mu_one=False)
+    E, B = tet_mass_stiffness_matrices(field, er, ur)
+    Eo, Bo = oracle.tet_mass_stiffness_matrices(field, er, ur)
+    assert rel_to_rowmax(E, Eo) <= TOL
+    assert rel_to_rowmax(B, Bo) <= TOL
