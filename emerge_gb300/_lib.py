@@ -29,6 +29,25 @@ SIGNATURES = {
     "emg_assemble_tet": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "emg_assemble_tet_host": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "emg_plan_destroy": (None, [c_vp]),
+    "emg_tri_robin_force": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                           c_vp, c_vp, c_vp]),
+    "emg_tri_robin_abc": (ctypes.c_int, [c_i64, c_vp, c_vp, ctypes.c_double, ctypes.c_double, c_vp, c_vp]),
+    "emg_csr_positions": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "emg_segment_add": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_double, c_vp, c_vp]),
+    "emg_combine": (ctypes.c_int, [c_i64, c_vp, c_vp, ctypes.c_double, c_vp, c_vp]),
+    "emg_rplan_create": (ctypes.c_int, [c_i64, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, ctypes.POINTER(c_vp)]),
+    "emg_rplan_n": (c_i64, [c_vp]),
+    "emg_rplan_nnz": (c_i64, [c_vp]),
+    "emg_rplan_levels": (c_i64, [c_vp]),
+    "emg_rplan_destroy": (None, [c_vp]),
+    "emg_rplan_form": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "emg_ilu0": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp]),
+    "emg_ilu_apply": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "emg_spmv": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "emg_rplan_gather": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "emg_rplan_scatter": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "emg_gmres": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_double, c_vp, c_vp, c_vp]),
     "emg_csr_pattern_noalloc": (ctypes.c_int, [c_i64, c_i64, c_vp, c_vp, c_vp, c_i64, c_i64p, c_vp]),
 }
 

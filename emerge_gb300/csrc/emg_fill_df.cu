@@ -64,15 +64,17 @@ __device__ __forceinline__ df operator*(df a, float c) {
 }
 __device__ __forceinline__ df operator*(float c, df a) { return a * c; }
 
-// hi + lo rounded (toward zero in the last bit) to FP64, with integer instructions.
-// Requires |lo| <= ulp(hi)/2 (every df op above renormalises).
+// hi + lo rounded (toward zero in the last bit) to FP64 with integer instructions
+// only (no FP64 pipe).  Requires |lo| <= ulp(hi)/2 (every df op renormalises).
+// Subnormal hi (|x| < 2^-126) is returned as a signed zero.
 __device__ __forceinline__ double to_double(df a) {
     const unsigned hb = __float_as_uint(a.h);
     const unsigned eh = (hb >> 23) & 0xffu;
-    if (eh == 0u || eh == 0xffu) return (double)a.h + (double)a.l;   // zero, subnormal, inf, nan
-    const unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
-                                    ((unsigned long long)(eh + 896u) << 52) |
-                                    ((unsigned long long)(hb & 0x7fffffu) << 29);
+    const unsigned long long sign = (unsigned long long)(hb & 0x80000000u) << 32;
+    if (eh == 0u) return __longlong_as_double((long long)sign);
+    const unsigned long long mant = (unsigned long long)(hb & 0x7fffffu) << 29;
+    if (eh == 0xffu) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull | mant));
+    const unsigned long long bits = sign | ((unsigned long long)(eh + 896u) << 52) | mant;
     const unsigned lb = __float_as_uint(a.l);
     const unsigned el = (lb >> 23) & 0xffu;
     if (el == 0u) return __longlong_as_double((long long)bits);
@@ -80,9 +82,25 @@ __device__ __forceinline__ double to_double(df a) {
     const bool opp = ((lb ^ hb) & 0x80000000u) != 0u;
     // position of lo's last mantissa bit in units of hi's FP64 ulp; one more when
     // subtracting from an exact power of two (the result is in the lower binade)
-    int sh = (int)el - (int)eh + 29 + ((opp && (hb & 0x7fffffu) == 0u) ? 1 : 0);
+    const int sh = (int)el - (int)eh + 29 + ((opp && (hb & 0x7fffffu) == 0u) ? 1 : 0);
     const long long add = sh >= 0 ? (m << sh) : (sh > -40 ? (m >> -sh) : 0ll);
     return __longlong_as_double((long long)(opp ? bits - (unsigned long long)add : bits + (unsigned long long)add));
+}
+
+// Compensated accumulator: running float sum plus running error, renormalised once.
+struct acc {
+    float s, e;
+};
+__device__ __forceinline__ void acc_fma(acc& a, df x, df y) {   // a += x * y
+    const float p = __fmul_rn(x.h, y.h);
+    float pe = __fmaf_rn(x.h, y.h, -p);
+    pe = __fmaf_rn(x.h, y.l, pe);
+    pe = __fmaf_rn(x.l, y.h, pe);
+    const float t = __fadd_rn(a.s, p);
+    const float bb = __fsub_rn(t, a.s);
+    const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+    a.s = t;
+    a.e = __fadd_rn(a.e, __fadd_rn(err, pe));
 }
 
 __device__ __forceinline__ df split(double x) {
@@ -324,15 +342,21 @@ __device__ void blk_ff(const Tet& T, const float* vt, uint64_t lm, int fi, int f
 constexpr int kWarps = 4;
 constexpr int kKmax = kDfMaxInc;        // incidences per warp group
 constexpr int kNmax = kDfMaxCols;       // columns per entity
+constexpr int kGmax = 6;                // entities per warp group
+constexpr int kColPool = 384;           // columns of all entities of a group
 
 struct __align__(16) WarpSm {
     float4 stage[kKmax * 10][4];        // per item: D (4 df) then F (4 df)
     float4 sc[kKmax][2];                // per incidence: sE, sB (re.h, re.l, im.h, im.l)
-    int32_t cols[2][kNmax];
+    int64_t b1[kGmax], b2[kGmax];       // CSR offsets of each entity's two rows
+    int32_t cols[kColPool];             // sorted columns of each entity (pooled)
+    int32_t n[kGmax], k[kGmax], cofs[kGmax], kofs[kGmax];
     int32_t tet[kKmax];
     int8_t slot[kKmax];
+    int8_t qent[kKmax];                 // entity (within the group) of each incidence
     uint8_t tab[kKmax][kNmax];          // (column slot j | column mode << 4) or 0xff
 };
+constexpr size_t kFillSmem = sizeof(WarpSm) * kWarps + 625 * sizeof(float);
 
 __device__ __forceinline__ int find_col(const int32_t* cols, int n, int32_t c) {
     int lo = 0, hi = n - 1;
@@ -348,48 +372,64 @@ __device__ __forceinline__ void store_df(float4* dst, const df X[2][2]) {
     dst[1] = make_float4(X[1][0].h, X[1][0].l, X[1][1].h, X[1][1].l);
 }
 
-__global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict__ recs, const int32_t* __restrict__ groups,
-                                                         int64_t n_groups, const int32_t* __restrict__ partner,
+// groups[g] = (first index into gents, entity count); all entities of a group are
+// the same kind (edges or faces) and together have at most kKmax incidences.
+__global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict__ recs, const int2* __restrict__ groups,
+                                                         int64_t n_groups, const int32_t* __restrict__ gents,
+                                                         const int32_t* __restrict__ partner,
                                                          const int64_t* __restrict__ inc_ptr, const int64_t* __restrict__ inc,
                                                          const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
                                                          const float4* __restrict__ tscale, double2* __restrict__ E,
                                                          double2* __restrict__ B) {
-    __shared__ float vt[625];
-    __shared__ WarpSm sm_all[kWarps];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    WarpSm* sm_all = reinterpret_cast<WarpSm*>(smem_raw);
+    float* vt = reinterpret_cast<float*>(smem_raw + sizeof(WarpSm) * kWarps);
     for (int i = threadIdx.x; i < 625; i += blockDim.x) vt[i] = c_vint[i];
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpSm& sm = sm_all[w];
     for (int64_t g = blockIdx.x * (int64_t)kWarps + w; g < n_groups; g += (int64_t)gridDim.x * kWarps) {
-        const int32_t ent[2] = {groups[2 * g], groups[2 * g + 1]};
-        const int nsub = ent[1] >= 0 ? 2 : 1;
-        int64_t b1[2], b2[2], i0[2];
-        int n[2], k[2], kofs[2];
-        int ktot = 0;
+        const int2 gr = groups[g];
+        const int nsub = gr.y;
+        // per-entity metadata (lane u handles entity u), then prefix offsets by lane 0
+        if (lane < nsub) {
+            const int32_t r1 = gents[gr.x + lane];
+            sm.b1[lane] = indptr[r1];
+            sm.b2[lane] = indptr[partner[r1]];
+            sm.n[lane] = (int)(indptr[r1 + 1] - indptr[r1]);
+            sm.k[lane] = (int)(inc_ptr[r1 + 1] - inc_ptr[r1]);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            int co = 0, ko = 0;
+            for (int u = 0; u < nsub; ++u) {
+                sm.cofs[u] = co;
+                sm.kofs[u] = ko;
+                co += sm.n[u];
+                ko += sm.k[u];
+            }
+        }
+        __syncwarp();
+        const int ktot = sm.kofs[nsub - 1] + sm.k[nsub - 1];
         for (int u = 0; u < nsub; ++u) {
-            const int32_t r1 = ent[u];
-            b1[u] = indptr[r1];
-            b2[u] = indptr[partner[r1]];
-            n[u] = (int)(indptr[r1 + 1] - b1[u]);
-            i0[u] = inc_ptr[r1];
-            k[u] = (int)(inc_ptr[r1 + 1] - i0[u]);
-            kofs[u] = ktot;
-            ktot += k[u];
+            const int64_t b1 = sm.b1[u];
+            const int n = sm.n[u], co = sm.cofs[u];
+            for (int c = lane; c < n; c += 32) sm.cols[co + c] = __ldg(indices + b1 + c);
+            const int32_t r1 = gents[gr.x + u];
+            const int64_t i0 = inc_ptr[r1];
+            const int ko = sm.kofs[u];
+            for (int q = lane; q < sm.k[u]; q += 32) {
+                const int64_t code = inc[i0 + q];
+                const int64_t t = code >> 4;
+                sm.tet[ko + q] = (int32_t)t;
+                sm.slot[ko + q] = (int8_t)(code & 15);
+                sm.qent[ko + q] = (int8_t)u;
+                sm.sc[ko + q][0] = __ldg(tscale + 2 * t);
+                sm.sc[ko + q][1] = __ldg(tscale + 2 * t + 1);
+            }
+            for (int q = 0; q < sm.k[u]; ++q)
+                for (int c = lane; c < n; c += 32) sm.tab[ko + q][c] = 0xff;
         }
-        for (int u = 0; u < nsub; ++u)
-            for (int c = lane; c < n[u]; c += 32) sm.cols[u][c] = __ldg(indices + b1[u] + c);
-        for (int q = lane; q < ktot; q += 32) {
-            const int u = (nsub == 2 && q >= kofs[1]) ? 1 : 0;
-            const int64_t code = inc[i0[u] + (q - kofs[u])];
-            const int64_t t = code >> 4;
-            sm.tet[q] = (int32_t)t;
-            sm.slot[q] = (int8_t)(code & 15);
-            sm.sc[q][0] = __ldg(tscale + 2 * t);
-            sm.sc[q][1] = __ldg(tscale + 2 * t + 1);
-        }
-        for (int u = 0; u < nsub; ++u)
-            for (int q = 0; q < k[u]; ++q)
-                for (int c = lane; c < n[u]; c += 32) sm.tab[kofs[u] + q][c] = 0xff;
         __syncwarp();
         // phase A: edge columns (j = 0..5); phase B: face columns (j = 6..9)
         for (int ph = 0; ph < 2; ++ph) {
@@ -417,23 +457,25 @@ __global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict_
                 float4* st = sm.stage[q * 10 + j];
                 store_df(st, D);
                 store_df(st + 2, F);
-                const int u = (nsub == 2 && q >= kofs[1]) ? 1 : 0;
-                const int p1 = find_col(sm.cols[u], n[u], __ldg(&rp->dof[j]));
-                const int p2 = find_col(sm.cols[u], n[u], __ldg(&rp->dof[j + 10]));
+                const int u = sm.qent[q];
+                const int32_t* cu = sm.cols + sm.cofs[u];
+                const int p1 = find_col(cu, sm.n[u], __ldg(&rp->dof[j]));
+                const int p2 = find_col(cu, sm.n[u], __ldg(&rp->dof[j + 10]));
                 sm.tab[q][p1] = (uint8_t)j;
                 sm.tab[q][p2] = (uint8_t)(j | 16);
             }
         }
         __syncwarp();
-        // owner phase
+        // owner phase: position-parallel accumulation in ascending tet order
         for (int u = 0; u < nsub; ++u) {
+            const int n = sm.n[u], ko = sm.kofs[u], ke = ko + sm.k[u];
             bool e_real = true;
-            for (int q = kofs[u]; q < kofs[u] + k[u]; ++q) e_real &= (sm.sc[q][0].z == 0.f && sm.sc[q][0].w == 0.f);
-            for (int p = lane; p < n[u]; p += 32) {
+            for (int q = ko; q < ke; ++q) e_real &= (sm.sc[q][0].z == 0.f && sm.sc[q][0].w == 0.f);
+            for (int p = lane; p < n; p += 32) {
 #pragma unroll
                 for (int a = 0; a < 2; ++a) {
-                    df er = mk(0.f, 0.f), ei = mk(0.f, 0.f), br = mk(0.f, 0.f), bi = mk(0.f, 0.f);
-                    for (int q = kofs[u]; q < kofs[u] + k[u]; ++q) {
+                    acc er = {0.f, 0.f}, ei = {0.f, 0.f}, br = {0.f, 0.f}, bi = {0.f, 0.f};
+                    for (int q = ko; q < ke; ++q) {
                         const uint8_t x = sm.tab[q][p];
                         if (x == 0xff) continue;
                         const int j = x & 15, b = x >> 4;
@@ -443,14 +485,14 @@ __global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict_
                         const df Dv = b ? mk(dv.z, dv.w) : mk(dv.x, dv.y);
                         const df Fv = b ? mk(fvv.z, fvv.w) : mk(fvv.x, fvv.y);
                         const float4 se = sm.sc[q][0], sb = sm.sc[q][1];
-                        er = er + mk(se.x, se.y) * Dv;
-                        if (!e_real) ei = ei + mk(se.z, se.w) * Dv;
-                        br = br + mk(sb.x, sb.y) * Fv;
-                        bi = bi + mk(sb.z, sb.w) * Fv;
+                        acc_fma(er, mk(se.x, se.y), Dv);
+                        if (!e_real) acc_fma(ei, mk(se.z, se.w), Dv);
+                        acc_fma(br, mk(sb.x, sb.y), Fv);
+                        acc_fma(bi, mk(sb.z, sb.w), Fv);
                     }
-                    const int64_t o = (a == 0 ? b1[u] : b2[u]) + p;
-                    E[o] = make_double2(to_double(er), e_real ? 0.0 : to_double(ei));
-                    B[o] = make_double2(to_double(br), to_double(bi));
+                    const int64_t o = (a == 0 ? sm.b1[u] : sm.b2[u]) + p;
+                    E[o] = make_double2(to_double(fts(er.s, er.e)), e_real ? 0.0 : to_double(fts(ei.s, ei.e)));
+                    B[o] = make_double2(to_double(fts(br.s, br.e)), to_double(fts(bi.s, bi.e)));
                 }
             }
         }
@@ -459,11 +501,10 @@ __global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict_
 }
 
 // ---------------------------------------------------- plan-time grouping ---
-// Classify entities: fast edges (k <= kKmax, n <= kNmax), fast faces (pairs),
-// everything else to the FP64 fallback list.
+// Entity classes: 0 edge with k <= kKmax/2 (two per group), 1 edge with
+// kKmax/2 < k <= kKmax (one per group), 2 face (kGmax per group), 3 FP64 fallback.
 __global__ void k_classify(const int32_t* __restrict__ ent_list, int64_t n_ent, const int64_t* __restrict__ inc_ptr,
-                           const int64_t* __restrict__ inc, const int64_t* __restrict__ indptr, int64_t* fe,
-                           int64_t* ff, int64_t* fs) {
+                           const int64_t* __restrict__ inc, const int64_t* __restrict__ indptr, int64_t* flags) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_ent; e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t r = ent_list[e];
         const int64_t k = inc_ptr[r + 1] - inc_ptr[r];
@@ -475,27 +516,36 @@ __global__ void k_classify(const int32_t* __restrict__ ent_list, int64_t n_ent, 
             if (kind < 0) kind = kk;
             uniform &= (kk == kind);
         }
-        const bool fits = uniform && n <= kNmax && ((kind == 0 && k <= kKmax) || (kind == 1 && k <= kKmax / 2));
-        fe[e] = (fits && kind == 0) ? 1 : 0;
-        ff[e] = (fits && kind == 1) ? 1 : 0;
-        fs[e] = fits ? 0 : 1;
+        int cls = 3;
+        if (uniform && kind == 0 && n <= kNmax && k <= kKmax / 2) cls = 0;
+        else if (uniform && kind == 0 && n <= kNmax && k <= kKmax) cls = 1;
+        else if (uniform && kind == 1 && n <= kColPool / kGmax && k <= kKmax / kGmax) cls = 2;
+        for (int c = 0; c < 4; ++c) flags[c * (n_ent + 1) + e] = (c == cls) ? 1 : 0;
     }
 }
 
-__global__ void k_groups(const int32_t* __restrict__ ent_list, int64_t n_ent, const int64_t* fe, const int64_t* fe_scan,
-                         const int64_t* ff, const int64_t* ff_scan, const int64_t* fs, const int64_t* fs_scan,
-                         int64_t n_fe, int32_t* groups, int32_t* slow) {
+// Scatter entities into the class-ordered list and write the groups.
+__global__ void k_groups(const int32_t* __restrict__ ent_list, int64_t n_ent, const int64_t* flags,
+                         const int64_t* scans, int64_t c0, int64_t c1, int64_t c2, int32_t* gents, int2* groups,
+                         int32_t* slow) {
+    const int64_t g0 = (c0 + 1) / 2, g1 = c1;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_ent; e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t r = ent_list[e];
-        if (fe[e]) {
-            const int64_t g = fe_scan[e];
-            groups[2 * g] = r;
-            groups[2 * g + 1] = -1;
-        } else if (ff[e]) {
-            const int64_t f = ff_scan[e];
-            groups[2 * (n_fe + f / 2) + (f & 1)] = r;
+        if (flags[e]) {
+            const int64_t i = scans[e];
+            gents[i] = r;
+            if ((i & 1) == 0) groups[i / 2] = make_int2((int)i, (int)(c0 - i < 2 ? c0 - i : 2));
+        } else if (flags[(n_ent + 1) + e]) {
+            const int64_t i = scans[(n_ent + 1) + e];
+            gents[c0 + i] = r;
+            groups[g0 + i] = make_int2((int)(c0 + i), 1);
+        } else if (flags[2 * (n_ent + 1) + e]) {
+            const int64_t i = scans[2 * (n_ent + 1) + e];
+            gents[c0 + c1 + i] = r;
+            if (i % kGmax == 0)
+                groups[g0 + g1 + i / kGmax] = make_int2((int)(c0 + c1 + i), (int)(c2 - i < kGmax ? c2 - i : kGmax));
         } else {
-            slow[fs_scan[e]] = r;
+            slow[scans[3 * (n_ent + 1) + e]] = r;
         }
     }
 }
@@ -532,6 +582,7 @@ void df_plan_free(DfPlan* p) {
     dfree(p->gscale);
     dfree(p->tscale);
     dfree(p->groups);
+    dfree(p->gents);
     dfree(p->slow);
     p->n_groups = p->n_slow = 0;
 }
@@ -544,67 +595,53 @@ int df_plan_build(const double* nodes, int64_t nN, const int32_t* tets, int64_t 
     if (rc) return rc;
     *p = DfPlan();
     int* d_err = nullptr;
-    int64_t *fe = nullptr, *ff = nullptr, *fs = nullptr, *fe_s = nullptr, *ff_s = nullptr, *fs_s = nullptr, *tmp = nullptr;
-    auto cleanup = [&]() {
-        dfree(d_err); dfree(fe); dfree(ff); dfree(fs); dfree(fe_s); dfree(ff_s); dfree(fs_s); dfree(tmp);
-    };
+    int64_t *flags = nullptr, *scans = nullptr, *tmp = nullptr;
+    auto cleanup = [&]() { dfree(d_err); dfree(flags); dfree(scans); dfree(tmp); };
 #define TRY(x) do { int _r = (x); if (_r) { cleanup(); df_plan_free(p); return _r; } } while (0)
+#define TRYC(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { cleanup(); df_plan_free(p); return cuda_status(_e, #x); } } while (0)
     TRY(dalloc(&d_err, 1, "df err"));
     TRY(dalloc(reinterpret_cast<dfk::Rec2**>(&p->recs), nT, "df records"));
     TRY(dalloc(&p->gscale, nT, "df geometric scales"));
     TRY(dalloc(&p->tscale, 2 * nT, "df material scales"));
-    {
-        const cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), s);
-        if (e != cudaSuccess) TRY(cuda_status(e, "memset"));
-    }
+    TRYC(cudaMemsetAsync(d_err, 0, sizeof(int), s));
     const int T = 256;
     if (nT > 0) {
         dfk::k_prep2<<<grid_for(nT, T), T, 0, s>>>(nodes, nN, tets, nT, edges, nE, tris, nTri, t2f, t2e, edge_len,
                                                    reinterpret_cast<dfk::Rec2*>(p->recs), p->gscale, d_err);
-        const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) TRY(cuda_status(e, "k_prep2"));
+        TRYC(cudaGetLastError());
     }
-    TRY(dalloc(&fe, n_ent + 1, "fe"));
-    TRY(dalloc(&ff, n_ent + 1, "ff"));
-    TRY(dalloc(&fs, n_ent + 1, "fs"));
-    TRY(dalloc(&fe_s, n_ent + 1, "fe scan"));
-    TRY(dalloc(&ff_s, n_ent + 1, "ff scan"));
-    TRY(dalloc(&fs_s, n_ent + 1, "fs scan"));
-    TRY(dalloc(&tmp, scan_scratch_elems(n_ent + 1) + 1, "scan tmp"));
+    const int64_t L = n_ent + 1;
+    TRY(dalloc(&flags, 4 * L, "df class flags"));
+    TRY(dalloc(&scans, 4 * L, "df class scans"));
+    TRY(dalloc(&tmp, scan_scratch_elems(L) + 1, "df scan scratch"));
     if (n_ent > 0) {
-        dfk::k_classify<<<grid_for(n_ent, T), T, 0, s>>>(ent_list, n_ent, inc_ptr, inc, indptr, fe, ff, fs);
-        const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) TRY(cuda_status(e, "k_classify"));
+        dfk::k_classify<<<grid_for(n_ent, T), T, 0, s>>>(ent_list, n_ent, inc_ptr, inc, indptr, flags);
+        TRYC(cudaGetLastError());
     }
-    TRY(scan_exclusive_i64(fe, fe_s, n_ent, tmp, s));
-    TRY(scan_exclusive_i64(ff, ff_s, n_ent, tmp, s));
-    TRY(scan_exclusive_i64(fs, fs_s, n_ent, tmp, s));
-    int64_t cnt[3] = {0, 0, 0};
+    for (int c = 0; c < 4; ++c) TRY(scan_exclusive_i64(flags + c * L, scans + c * L, n_ent, tmp, s));
+    int64_t cnt[4] = {0, 0, 0, 0};
     int h_err = 0;
-    if (cudaMemcpyAsync(&cnt[0], fe_s + n_ent, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(&cnt[1], ff_s + n_ent, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(&cnt[2], fs_s + n_ent, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-        TRY(cuda_status(cudaGetLastError(), "df plan readback"));
+    for (int c = 0; c < 4; ++c)
+        TRYC(cudaMemcpyAsync(&cnt[c], scans + c * L + n_ent, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    TRYC(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TRYC(cudaStreamSynchronize(s));
     if (h_err) {
         set_error("mesh check failed: an edge/face vertex is not a vertex of its tet");
         TRY(EMG_ERR_MESH);
     }
-    p->n_groups = cnt[0] + (cnt[1] + 1) / 2;
-    p->n_slow = cnt[2];
-    TRY(dalloc(&p->groups, 2 * p->n_groups + 2, "df groups"));
+    p->n_groups = (cnt[0] + 1) / 2 + cnt[1] + (cnt[2] + dfk::kGmax - 1) / dfk::kGmax;
+    p->n_slow = cnt[3];
+    TRY(dalloc(&p->groups, p->n_groups + 1, "df groups"));
+    TRY(dalloc(&p->gents, cnt[0] + cnt[1] + cnt[2] + 1, "df group entities"));
     TRY(dalloc(&p->slow, p->n_slow + 1, "df slow list"));
-    if (p->n_groups > 0 && cudaMemsetAsync(p->groups, 0xff, sizeof(int32_t) * (2 * p->n_groups + 2), s) != cudaSuccess)
-        TRY(cuda_status(cudaGetLastError(), "memset groups"));
     if (n_ent > 0) {
-        dfk::k_groups<<<grid_for(n_ent, T), T, 0, s>>>(ent_list, n_ent, fe, fe_s, ff, ff_s, fs, fs_s, cnt[0], p->groups,
-                                                        p->slow);
-        const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) TRY(cuda_status(e, "k_groups"));
+        dfk::k_groups<<<grid_for(n_ent, T), T, 0, s>>>(ent_list, n_ent, flags, scans, cnt[0], cnt[1], cnt[2], p->gents,
+                                                        p->groups, p->slow);
+        TRYC(cudaGetLastError());
     }
-    if (cudaStreamSynchronize(s) != cudaSuccess) TRY(cuda_status(cudaGetLastError(), "df plan sync"));
+    TRYC(cudaStreamSynchronize(s));
 #undef TRY
+#undef TRYC
     cleanup();
     return EMG_OK;
 }
@@ -612,6 +649,14 @@ int df_plan_build(const double* nodes, int64_t nN, const int32_t* tets, int64_t 
 int df_fill(const DfPlan& p, int64_t nT, const int32_t* partner, const int64_t* inc_ptr, const int64_t* inc,
             const int64_t* indptr, const int32_t* indices, const double* eps, const double* mu_inv, double* E,
             double* B, cudaStream_t s) {
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    EMG_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        EMG_CUDA(cudaFuncSetAttribute(dfk::k_fill_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)dfk::kFillSmem));
+        attr_set[dev] = true;
+    }
     if (nT > 0) {
         dfk::k_scales<<<grid_for(nT, 256), 256, 0, s>>>(p.gscale, reinterpret_cast<const double2*>(eps),
                                                          reinterpret_cast<const double2*>(mu_inv), nT, p.tscale);
@@ -619,9 +664,10 @@ int df_fill(const DfPlan& p, int64_t nT, const int32_t* partner, const int64_t* 
     }
     if (p.n_groups > 0) {
         const unsigned g = grid_for(p.n_groups, dfk::kWarps, 152u * 32u);
-        dfk::k_fill_df<<<g, 32 * dfk::kWarps, 0, s>>>(reinterpret_cast<const dfk::Rec2*>(p.recs), p.groups, p.n_groups,
-                                                       partner, inc_ptr, inc, indptr, indices, p.tscale,
-                                                       reinterpret_cast<double2*>(E), reinterpret_cast<double2*>(B));
+        dfk::k_fill_df<<<g, 32 * dfk::kWarps, dfk::kFillSmem, s>>>(
+            reinterpret_cast<const dfk::Rec2*>(p.recs), reinterpret_cast<const int2*>(p.groups), p.n_groups, p.gents,
+            partner, inc_ptr, inc, indptr, indices, p.tscale, reinterpret_cast<double2*>(E),
+            reinterpret_cast<double2*>(B));
         EMG_CUDA(cudaGetLastError());
     }
     return EMG_OK;

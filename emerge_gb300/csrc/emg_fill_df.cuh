@@ -14,7 +14,8 @@ struct DfPlan {
     void* recs = nullptr;        // per-tet normalised float-float invariants (448 B/tet)
     double2* gscale = nullptr;   // per-tet FP64 scales of the curl-curl and mass blocks
     float4* tscale = nullptr;    // per-tet complex material scales (written by each fill)
-    int32_t* groups = nullptr;   // warp work units: (edge entity, -1) or (face entity, face entity | -1)
+    int2* groups = nullptr;      // warp work units: (first index into gents, entity count)
+    int32_t* gents = nullptr;    // fast-fill entities ordered by class (2 edges / 1 edge / 6 faces per unit)
     int32_t* slow = nullptr;     // entities outside the fast-fill limits (FP64 fill)
     int64_t n_groups = 0;
     int64_t n_slow = 0;

@@ -80,6 +80,94 @@ int emg_assemble_tet_host(emg_plan* plan, const double* eps, const double* mu_in
 /* Releases the plan and its device memory. */
 void emg_plan_destroy(emg_plan* plan);
 
+/* ------------------------------------------------------- surface terms ---
+ * Replace the per-triangle Robin kernels behind assemble_robin_bc_excited /
+ * assemble_robin_bc (fem/physics/edm/assembler.py:83-144).  One thread per
+ * triangle, FP64.  All arrays are DEVICE arrays, complex = interleaved doubles.
+ */
+
+/* ned2_tri_stiff_force (fem/mth/tri.py:575-695) for n_tris waveport triangles:
+ * lcs_xy (2, 3, n_tris): local x and y of each triangle's three vertices (tri
+ * vertex order) = rows 0-1 of local_basis @ (nodes - origin); uinc
+ * (3, npts, n_tris) complex: U_inc at the quadrature points of each triangle;
+ * dpts (4, npts): weights and barycentrics (gaus_quad_tri(4): npts = 6).
+ * Outputs B_out (n_tris, 8, 8) and b_out (n_tris, 8), complex, gamma applied. */
+int emg_tri_robin_force(int64_t n_tris, const double* lcs_xy, const double* uinc, const double* dpts, int npts,
+                        double gamma_re, double gamma_im, double* B_out, double* b_out, void* stream);
+
+/* ned2_tri_stiff (fem/mth/tri.py:697-797) for n_tris absorbing-boundary
+ * triangles: xyz (3, 3, n_tris) = coordinate c of vertex k at [c][k][t];
+ * edge_lengths (3, n_tris) of the edges (v0v1, v1v2, v0v2).  B_out (n_tris, 8, 8). */
+int emg_tri_robin_abc(int64_t n_tris, const double* xyz, const double* edge_lengths, double gamma_re,
+                      double gamma_im, double* B_out, void* stream);
+
+/* pos[i] = position of column cols[i] within CSR row rows[i] of (indptr,
+ * indices), -1 if the pair is not in the pattern. */
+int emg_csr_positions(int64_t n, const int32_t* rows, const int32_t* cols, const int64_t* indptr,
+                      const int32_t* indices, int64_t* pos, void* stream);
+
+/* Deterministic scatter-add: for each segment s,
+ * out[dst[s]] += alpha * sum(src[perm[k]] for k in [seg_ptr[s], seg_ptr[s+1])),
+ * summed in perm order (complex).  Replaces the duplicate summation of
+ * coo_matrix(...).tocsr() and the ``K + B_p`` / ``Bvec[indices] += bvec`` updates. */
+int emg_segment_add(int64_t n_seg, const int64_t* seg_ptr, const int64_t* perm, const int64_t* dst,
+                    const double* src, double alpha_re, double alpha_im, double* out, void* stream);
+
+/* K = E - k0sq * B on a shared CSR pattern (fem/physics/edm/assembler.py:333). */
+int emg_combine(int64_t nnz, const double* E, const double* B, double k0sq, double* K, void* stream);
+
+/* ------------------------------------------------------------- solver ---
+ * Replaces the solve of SolveRoutine.solve (fem/solver.py:405-469): restriction
+ * to solve_ids (solver.py:434-435), the sparse solve (SuperLU / PARDISO / GMRES,
+ * solver.py:220-309) and the scatter back with zeros on PEC DOFs
+ * (solver.py:465).  Batched: Bc right-hand-side columns, column c solved with
+ * stored matrix cmat[c] of Bm.  Layouts: matrices [nnz_r][Bm], vectors
+ * [n_solve][Bc], complex interleaved, DEVICE arrays unless stated.
+ */
+typedef struct emg_rplan emg_rplan;
+
+/* Restricted pattern A[ix_(solve_ids, solve_ids)] of a full CSR pattern
+ * (indptr int64 N+1, indices int32), ILU(0) level schedule and update lists.
+ * Synchronises ``stream``. */
+int emg_rplan_create(int64_t N, const int64_t* indptr, const int32_t* indices, int64_t nnz_full, int64_t n_solve,
+                     const int64_t* solve_ids, void* stream, emg_rplan** plan);
+int64_t emg_rplan_n(const emg_rplan* plan);
+int64_t emg_rplan_nnz(const emg_rplan* plan);
+int64_t emg_rplan_levels(const emg_rplan* plan);
+void emg_rplan_destroy(emg_rplan* plan);
+
+/* Restricted matrices A_m = E - k2[m] B + sum_p gam[p][m] P_p (m < Bm) from
+ * full-pattern values E, B (nnz_full complex), unit port matrices P
+ * (n_ports x nnz_full complex), k2 (Bm doubles), gam (n_ports x Bm complex).
+ * Forms K(k0) of fem/physics/edm/assembler.py:333,382-383 for Bm frequencies. */
+int emg_rplan_form(const emg_rplan* plan, int64_t Bm, const double* E, const double* B, const double* k2,
+                   int64_t n_ports, const double* P, const double* gam, double* A, void* stream);
+
+/* In-place ILU(0) of Bm matrices (LU holds a copy of A on entry). */
+int emg_ilu0(const emg_rplan* plan, int64_t Bm, double* LU, void* stream);
+
+/* X <- (LU)^-1 X (forward and backward level-scheduled substitution). */
+int emg_ilu_apply(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* LU, double* X,
+                  void* stream);
+
+/* Y = A X, or Y = Bv - A X when Bv is not NULL. */
+int emg_spmv(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A, const double* X,
+             const double* Bv, double* Y, void* stream);
+
+/* out[i][c] = full[c][solve_ids[i]] (full: Bc vectors of N) and the inverse
+ * scatter (zeros on removed DOFs). */
+int emg_rplan_gather(const emg_rplan* plan, int64_t Bc, const double* full, double* out, void* stream);
+int emg_rplan_scatter(const emg_rplan* plan, int64_t Bc, const double* x, double* full, void* stream);
+
+/* Right-preconditioned restarted GMRES(restart <= 64) with CGS2, columns in
+ * lockstep; x holds the initial guess on entry.  Stops a column at relative
+ * residual tol or after max_iter total iterations; iters_out (Bc int32) and
+ * resid_out (Bc doubles, explicit ||b - A x|| / ||b||) are DEVICE arrays.
+ * Synchronises ``stream``. */
+int emg_gmres(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A, const double* LU,
+              const double* rhs, double* x, int restart, int max_iter, double tol, int32_t* iters_out,
+              double* resid_out, void* stream);
+
 /* CSR pattern without any device allocation.  No counterpart in the reference:
  * an addition for callers that cannot call cudaMalloc, e.g. a host application
  * that must not allocate device memory of its own (its memory is owned by

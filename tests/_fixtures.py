@@ -24,7 +24,28 @@ def field_from(z) -> types.SimpleNamespace:
     mesh.n_tris = mesh.tris.shape[1]
     f = types.SimpleNamespace(mesh=mesh, tet_to_field=i8("tet_to_field"))
     f.n_field = 2 * mesh.n_edges + 2 * mesh.n_tris
+    nE, nF = mesh.n_edges, mesh.n_tris
+    f.edge_to_field = np.stack([np.arange(nE), np.arange(nE) + nF + nE]).astype(np.int64)
+    if "tri_to_field" in z:
+        f.tri_to_field = i8("tri_to_field")
     return f
+
+
+def waveguide_field_and_bcs(z):
+    """The WR-90 fixture as a field plus project BC objects mirroring the reference run."""
+    from emerge_gb300 import bc as pbc
+    from emerge_gb300 import mesh as pm
+    field = field_from(z)
+    a, b, L = (float(v) for v in z["dims"])
+    tag_tris = {(pm.FACE_YMIN,): z["port_tris_1"], (pm.FACE_YMAX,): z["port_tris_2"],
+                (pm.FACE_XMIN, pm.FACE_XMAX, pm.FACE_ZMIN, pm.FACE_ZMAX): z["pec_tris"]}
+    field.mesh.get_triangles = lambda tags: np.asarray(tag_tris[tuple(tags)], dtype=np.int64)
+    p1 = pbc.RectangularWaveguide([pm.FACE_YMIN], 1, pbc.CoordinateSystem([1.0, 0, 0], [0, 0, 1.0], [0, -1.0, 0],
+                                                                        [a / 2, 0.0, b / 2]), (a, b))
+    p2 = pbc.RectangularWaveguide([pm.FACE_YMAX], 2, pbc.CoordinateSystem([-1.0, 0, 0], [0, 0, 1.0], [0, 1.0, 0],
+                                                                        [a / 2, L, b / 2]), (a, b))
+    pec = pbc.PEC([pm.FACE_XMIN, pm.FACE_XMAX, pm.FACE_ZMIN, pm.FACE_ZMAX])
+    return field, [pec, p1, p2]
 
 
 def csr_from(z, prefix: str):
