@@ -1,0 +1,781 @@
+// Restricted frequency-domain systems and a batched ILU(0)-preconditioned GMRES.
+//
+// Replaces the solve behind SolveRoutine.solve (fem/solver.py:405-469):
+//   A[ix_(solve_ids, solve_ids)] restriction (solver.py:434-435), the linear
+//   solve itself (SuperLU/PARDISO/GMRES, solver.py:220-309), and the scatter of
+//   the solution back to all DOFs with zeros on PEC DOFs (solver.py:465).
+//
+// Batching: B right-hand-side columns are solved in lockstep; column c uses
+// matrix cmat[c] of Bm stored matrices.  A frequency sweep stores one matrix per
+// frequency, A(k) = E - k^2 B + sum_p gamma_p(k) P_p, formed from the volume
+// matrices and unit port matrices (every Robin block is linear in gamma), with
+// one column per (frequency, port).  Layouts put the batch index innermost so
+// that threads of a warp handle neighbouring columns of the same row and all
+// loads are coalesced: matrices [nnz][Bm], vectors [n][B] (complex double2).
+//
+// ILU(0) is level-scheduled: row i of L depends on the rows j < i it references,
+// so the rows of one level are factored/solved in parallel, one launch per
+// level.  The factorization update lists (which entries of row i row k of U
+// updates) are built once per pattern on the host.
+#include <algorithm>
+#include <vector>
+
+#include "emg_common.cuh"
+
+namespace emg {
+namespace kry {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) { return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }  // conj(a)*b
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+    const double d = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+// restricted pattern: count kept entries of each kept row
+__global__ void k_rcount(int64_t ns, const int64_t* __restrict__ sid, const int64_t* __restrict__ indptr,
+                         const int32_t* __restrict__ indices, const int32_t* __restrict__ map, int64_t* cnt) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < ns; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = sid[r];
+        int64_t c = 0;
+        for (int64_t k = indptr[row]; k < indptr[row + 1]; ++k) c += map[indices[k]] >= 0;
+        cnt[r] = c;
+    }
+}
+
+__global__ void k_rwrite(int64_t ns, const int64_t* __restrict__ sid, const int64_t* __restrict__ indptr,
+                         const int32_t* __restrict__ indices, const int32_t* __restrict__ map,
+                         const int64_t* __restrict__ rptr, int32_t* rind, int64_t* rsrc, int64_t* rdiag) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < ns; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = sid[r];
+        int64_t o = rptr[r];
+        rdiag[r] = -1;
+        for (int64_t k = indptr[row]; k < indptr[row + 1]; ++k) {
+            const int32_t m = map[indices[k]];
+            if (m < 0) continue;
+            rind[o] = m;
+            rsrc[o] = k;
+            if (m == r) rdiag[r] = o;
+            ++o;
+        }
+    }
+}
+
+__global__ void k_map(int64_t ns, const int64_t* __restrict__ sid, int32_t* map) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < ns; r += (int64_t)gridDim.x * blockDim.x)
+        map[sid[r]] = (int32_t)r;
+}
+
+// A[k][m] = E[s] - k2[m] B[s] + sum_p gam[p][m] P[p][s],  s = src[k]
+__global__ void k_form(int64_t nnz_r, int64_t Bm, const int64_t* __restrict__ src, const double2* __restrict__ E,
+                       const double2* __restrict__ B, const double* __restrict__ k2, int64_t n_ports,
+                       const double2* __restrict__ P, int64_t nnz_full, const double2* __restrict__ gam,
+                       double2* __restrict__ A) {
+    const int64_t total = nnz_r * Bm;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = t / Bm, m = t % Bm;
+        const int64_t s = src[k];
+        const double2 e = E[s], b = B[s];
+        double2 v = make_double2(e.x - k2[m] * b.x, e.y - k2[m] * b.y);
+        for (int64_t p = 0; p < n_ports; ++p) v = cadd(v, cmul(gam[p * Bm + m], P[p * nnz_full + s]));
+        A[t] = v;
+    }
+}
+
+// ILU(0) of the rows of one level, thread per (row, matrix).  For row i, in column
+// order: a_ik /= a_kk for each k < i, then a_ij -= a_ik a_kj over the update list.
+__global__ void k_ilu_level(int64_t nrows, const int32_t* __restrict__ rows, int64_t Bm,
+                            const int64_t* __restrict__ rptr, const int32_t* __restrict__ rind,
+                            const int64_t* __restrict__ rdiag, const int64_t* __restrict__ uptr,
+                            const int64_t* __restrict__ ulist, double2* __restrict__ LU) {
+    const int64_t total = nrows * Bm;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = rows[t / Bm], m = t % Bm;
+        int64_t u = uptr[i];
+        for (int64_t kk = rptr[i]; kk < rdiag[i]; ++kk) {
+            const int32_t k = rind[kk];
+            const double2 l = cdiv(LU[kk * Bm + m], LU[rdiag[k] * Bm + m]);
+            LU[kk * Bm + m] = l;
+            // update list entries for this kk: pairs (source position in row k, target in row i)
+            while (u < uptr[i + 1] && ulist[2 * u] >> 32 == kk - rptr[i]) {
+                const int64_t sk = ulist[2 * u] & 0xffffffffll, ti = ulist[2 * u + 1];
+                LU[ti * Bm + m] = csub(LU[ti * Bm + m], cmul(l, LU[sk * Bm + m]));
+                ++u;
+            }
+        }
+    }
+}
+
+// Level of forward (L) or backward (U) substitution: thread per (row, column).
+__global__ void k_trsv_level(int64_t nrows, const int32_t* __restrict__ rows, int64_t Bc, const int32_t* __restrict__ cmat,
+                             int64_t Bm, const int64_t* __restrict__ rptr, const int32_t* __restrict__ rind,
+                             const int64_t* __restrict__ rdiag, const double2* __restrict__ LU, int upper,
+                             double2* __restrict__ X) {
+    const int64_t total = nrows * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = rows[t / Bc], c = t % Bc;
+        const int64_t m = cmat[c];
+        double2 s = X[i * Bc + c];
+        if (!upper) {
+            for (int64_t k = rptr[i]; k < rdiag[i]; ++k) s = csub(s, cmul(LU[k * Bm + m], X[(int64_t)rind[k] * Bc + c]));
+            X[i * Bc + c] = s;
+        } else {
+            for (int64_t k = rdiag[i] + 1; k < rptr[i + 1]; ++k) s = csub(s, cmul(LU[k * Bm + m], X[(int64_t)rind[k] * Bc + c]));
+            X[i * Bc + c] = cdiv(s, LU[rdiag[i] * Bm + m]);
+        }
+    }
+}
+
+// Y = A X (batched, thread per (row, column)); alpha*A X + beta*Y when add.
+__global__ void k_spmv(int64_t n, int64_t Bc, const int32_t* __restrict__ cmat, int64_t Bm,
+                       const int64_t* __restrict__ rptr, const int32_t* __restrict__ rind, const double2* __restrict__ A,
+                       const double2* __restrict__ X, const double2* __restrict__ Bv, double2* __restrict__ Y) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / Bc, c = t % Bc;
+        const int64_t m = cmat[c];
+        double2 s = make_double2(0.0, 0.0);
+        for (int64_t k = rptr[i]; k < rptr[i + 1]; ++k) s = cadd(s, cmul(A[k * Bm + m], X[(int64_t)rind[k] * Bc + c]));
+        // Bv != nullptr: Y = Bv - A X (residual)
+        Y[t] = Bv ? csub(Bv[t], s) : s;
+    }
+}
+
+// Column-wise partial dots: part[blk][j][c] = sum_{rows in blk} conj(V_j[r,c]) W[r,c], j < nj.
+constexpr int kDotRows = 1024;
+constexpr int kMaxRestart = 256;
+__global__ void k_dots_partial(int64_t n, int64_t Bc, int nj, const double2* __restrict__ V, int64_t vstride,
+                               const double2* __restrict__ W, double2* __restrict__ part) {
+    const int64_t c = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= Bc) return;
+    const int64_t r0 = (int64_t)blockIdx.x * kDotRows, r1 = min(n, r0 + kDotRows);
+    for (int j = 0; j < nj; ++j) {
+        double2 s = make_double2(0.0, 0.0);
+        const double2* Vj = V + j * vstride;
+        for (int64_t r = r0; r < r1; ++r) s = cadd(s, cmulc(Vj[r * Bc + c], W[r * Bc + c]));
+        part[((int64_t)blockIdx.x * nj + j) * Bc + c] = s;
+    }
+}
+
+// Small batches (Bc < 32): warp per (vector j, column c) pair, lanes over rows.
+__global__ void k_dots_partial_small(int64_t n, int64_t Bc, int nj, const double2* __restrict__ V, int64_t vstride,
+                                     const double2* __restrict__ W, double2* __restrict__ part) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int64_t r0 = (int64_t)blockIdx.x * kDotRows, r1 = min(n, r0 + kDotRows);
+    for (int64_t pr = warp; pr < (int64_t)nj * Bc; pr += nw) {
+        const int64_t j = pr / Bc, c = pr % Bc;
+        const double2* Vj = V + j * vstride;
+        double2 s = make_double2(0.0, 0.0);
+        for (int64_t r = r0 + lane; r < r1; r += 32) s = cadd(s, cmulc(Vj[r * Bc + c], W[r * Bc + c]));
+        for (int o = 16; o > 0; o >>= 1) {
+            s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+            s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+        }
+        if (lane == 0) part[((int64_t)blockIdx.x * nj + j) * Bc + c] = s;
+    }
+}
+
+__global__ void k_dots_final(int64_t nblk, int64_t Bc, int nj, const double2* __restrict__ part, double2* __restrict__ out) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nj * Bc) return;
+    const int64_t j = t / Bc, c = t % Bc;
+    double2 s = make_double2(0.0, 0.0);
+    for (int64_t b = 0; b < nblk; ++b) s = cadd(s, part[(b * nj + j) * Bc + c]);
+    out[t] = s;
+}
+
+// W[r,c] -= sum_j h[j][c] V_j[r,c]   (masked columns untouched)
+__global__ void k_orth_update(int64_t n, int64_t Bc, int nj, const double2* __restrict__ V, int64_t vstride,
+                              const double2* __restrict__ h, const int32_t* __restrict__ active, double2* __restrict__ W) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = t % Bc;
+        if (!active[c]) continue;
+        double2 w = W[t];
+        for (int j = 0; j < nj; ++j) w = csub(w, cmul(h[(int64_t)j * Bc + c], V[j * vstride + t]));
+        W[t] = w;
+    }
+}
+
+// V_out[r,c] = W[r,c] * scale[c]
+__global__ void k_scale_cols(int64_t n, int64_t Bc, const double* __restrict__ scale, const double2* __restrict__ W,
+                             double2* __restrict__ Vout) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const double s = scale[t % Bc];
+        const double2 w = W[t];
+        Vout[t] = make_double2(w.x * s, w.y * s);
+    }
+}
+
+// X[r,c] += sum_j y[j][c] Z_j[r,c]   (masked by ``has``: columns with a nonzero update length)
+__global__ void k_combine_basis(int64_t n, int64_t Bc, int nj, const double2* __restrict__ Z, int64_t zstride,
+                                const double2* __restrict__ y, double2* __restrict__ X) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = t % Bc;
+        double2 x = X[t];
+        for (int j = 0; j < nj; ++j) x = cadd(x, cmul(y[(int64_t)j * Bc + c], Z[j * zstride + t]));
+        X[t] = x;
+    }
+}
+
+// Per column Arnoldi step bookkeeping (thread per column): append column j of H
+// (h[0..j] from two Gram-Schmidt passes, hn = ||w||), apply the stored Givens
+// rotations, make the new one, update g, decide convergence.
+__global__ void k_arnoldi_col(int64_t Bc, int j, int m, const double2* __restrict__ h1, const double2* __restrict__ h2,
+                              const double* __restrict__ wnorm2, double2* __restrict__ H, double2* __restrict__ cs,
+                              double2* __restrict__ sn, double2* __restrict__ g, const double* __restrict__ bnorm,
+                              double tol, int32_t* active, int32_t* len, double* vscale, double* resid) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= Bc) return;
+    if (!active[c]) { vscale[c] = 0.0; return; }
+    // column j of H: entries 0..j, then the subdiagonal
+    double2 col[kMaxRestart + 1];
+    for (int i = 0; i <= j; ++i) col[i] = cadd(h1[(int64_t)i * Bc + c], h2[(int64_t)i * Bc + c]);
+    const double hn = sqrt(fmax(wnorm2[c], 0.0));
+    col[j + 1] = make_double2(hn, 0.0);
+    for (int i = 0; i < j; ++i) {
+        const double2 ci = cs[(int64_t)i * Bc + c], si = sn[(int64_t)i * Bc + c];
+        // [c  s; -conj(s) c] with real-valued c stored in .x
+        const double2 a = col[i], b = col[i + 1];
+        col[i] = cadd(make_double2(ci.x * a.x, ci.x * a.y), cmul(si, b));
+        col[i + 1] = csub(make_double2(ci.x * b.x, ci.x * b.y), cmulc(si, a));
+    }
+    const double2 a = col[j], b = col[j + 1];
+    const double na = sqrt(a.x * a.x + a.y * a.y), nb = sqrt(b.x * b.x + b.y * b.y);
+    double cr;
+    double2 s;
+    if (nb == 0.0) { cr = 1.0; s = make_double2(0.0, 0.0); }
+    else if (na == 0.0) { cr = 0.0; s = make_double2(1.0, 0.0); }
+    else {
+        const double nr = sqrt(na * na + nb * nb);
+        cr = na / nr;
+        // s = (a/|a|) * conj(b) / nr
+        const double2 ua = make_double2(a.x / na, a.y / na);
+        s = cmul(ua, make_double2(b.x / nr, -b.y / nr));
+    }
+    cs[(int64_t)j * Bc + c] = make_double2(cr, 0.0);
+    sn[(int64_t)j * Bc + c] = s;
+    col[j] = cadd(make_double2(cr * a.x, cr * a.y), cmul(s, b));
+    col[j + 1] = make_double2(0.0, 0.0);
+    for (int i = 0; i <= j; ++i) H[((int64_t)i * m + j) * Bc + c] = col[i];
+    const double2 gj = g[(int64_t)j * Bc + c];
+    g[(int64_t)j * Bc + c] = make_double2(cr * gj.x, cr * gj.y);
+    g[(int64_t)(j + 1) * Bc + c] = make_double2(-(s.x * gj.x + s.y * gj.y), -(s.x * gj.y - s.y * gj.x));  // -conj(s)*g
+    const double2 gn = g[(int64_t)(j + 1) * Bc + c];
+    const double rn = sqrt(gn.x * gn.x + gn.y * gn.y);
+    resid[c] = rn / bnorm[c];
+    len[c] = j + 1;
+    vscale[c] = hn > 0.0 ? 1.0 / hn : 0.0;
+    if (rn <= tol * bnorm[c] || hn == 0.0) active[c] = 0;
+}
+
+// Back substitution H y = g per column (thread per column), lengths len[c].
+__global__ void k_backsolve(int64_t Bc, int m, const double2* __restrict__ H, const double2* __restrict__ g,
+                            const int32_t* __restrict__ len, double2* __restrict__ y, int nmax) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= Bc) return;
+    const int L = len[c];
+    for (int i = nmax - 1; i >= 0; --i) {
+        if (i >= L) { y[(int64_t)i * Bc + c] = make_double2(0.0, 0.0); continue; }
+        double2 s = g[(int64_t)i * Bc + c];
+        for (int k = i + 1; k < L; ++k) s = csub(s, cmul(H[((int64_t)i * m + k) * Bc + c], y[(int64_t)k * Bc + c]));
+        y[(int64_t)i * Bc + c] = cdiv(s, H[((int64_t)i * m + i) * Bc + c]);
+    }
+}
+
+// Per column: norms from the dots (|.|^2 sums), set up a restart: bnorm, g0, V0 scale, active.
+__global__ void k_restart_cols(int64_t Bc, const double2* __restrict__ rr, const double* __restrict__ bnorm, double tol,
+                               double2* __restrict__ g, double* __restrict__ vscale, int32_t* active, int32_t* len,
+                               double* resid, int64_t gstride) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= Bc) return;
+    const double rn = sqrt(fmax(rr[c].x, 0.0));
+    resid[c] = bnorm[c] > 0 ? rn / bnorm[c] : 0.0;
+    len[c] = 0;
+    const bool act = rn > tol * bnorm[c] && bnorm[c] > 0;
+    active[c] = act ? 1 : 0;
+    g[c] = make_double2(rn, 0.0);
+    for (int64_t i = 1; i < gstride; ++i) g[i * Bc + c] = make_double2(0.0, 0.0);
+    vscale[c] = act ? 1.0 / rn : 0.0;
+}
+
+__global__ void k_gather_rhs(int64_t ns, int64_t Bc, const int64_t* __restrict__ sid, int64_t N,
+                             const double2* __restrict__ full, double2* __restrict__ out) {
+    const int64_t total = ns * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / Bc, c = t % Bc;
+        out[t] = full[c * N + sid[i]];
+    }
+}
+
+__global__ void k_scatter_sol(int64_t ns, int64_t Bc, const int64_t* __restrict__ sid, int64_t N,
+                              const double2* __restrict__ x, double2* __restrict__ full) {
+    const int64_t total = ns * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / Bc, c = t % Bc;
+        full[c * N + sid[i]] = x[t];
+    }
+}
+
+__global__ void k_axpy1(int64_t nv, const double2* __restrict__ d, double2* __restrict__ x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nv; t += (int64_t)gridDim.x * blockDim.x)
+        x[t] = cadd(x[t], d[t]);
+}
+
+__global__ void k_real(int64_t Bc, const double2* __restrict__ in, double* __restrict__ out) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c < Bc) out[c] = in[c].x;
+}
+
+__global__ void k_sqrt_real(int64_t Bc, const double2* __restrict__ in, double* __restrict__ out) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c < Bc) out[c] = sqrt(fmax(in[c].x, 0.0));
+}
+
+}  // namespace kry
+}  // namespace emg
+
+// ------------------------------------------------------------------ plan ---
+struct emg_rplan {
+    int64_t N = 0, ns = 0, nnz = 0, nnz_full = 0;
+    int64_t* sid = nullptr;       // solve ids (ns)
+    int32_t* map = nullptr;       // full -> restricted (N), -1 if removed
+    int64_t* rptr = nullptr;      // (ns+1)
+    int32_t* rind = nullptr;      // (nnz)
+    int64_t* rsrc = nullptr;      // (nnz) positions in the full pattern
+    int64_t* rdiag = nullptr;     // (ns)
+    int64_t* uptr = nullptr;      // (ns+1) factorization update lists
+    int64_t* ulist = nullptr;     // pairs (kk_local << 32 | pos in row k, target pos)
+    int32_t* lrows = nullptr;     // rows by forward level
+    int32_t* urows = nullptr;     // rows by backward level
+    std::vector<int64_t> lptr, uptr_lv;   // level boundaries (host)
+    // GMRES workspace (grown on demand)
+    size_t ws_bytes = 0;
+    void* ws = nullptr;
+    // private stream for graph capture of the Arnoldi step (the caller's stream may be
+    // the legacy default stream, which cannot be captured)
+    cudaStream_t gs = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+};
+
+namespace {
+using namespace emg;
+
+void rplan_free(emg_rplan* p) {
+    if (!p) return;
+    dfree(p->sid); dfree(p->map); dfree(p->rptr); dfree(p->rind); dfree(p->rsrc); dfree(p->rdiag);
+    dfree(p->uptr); dfree(p->ulist); dfree(p->lrows); dfree(p->urows);
+    if (p->ws) cudaFree(p->ws);
+    if (p->ev_in) cudaEventDestroy(p->ev_in);
+    if (p->ev_out) cudaEventDestroy(p->ev_out);
+    if (p->gs) cudaStreamDestroy(p->gs);
+    delete p;
+}
+}  // namespace
+
+extern "C" int emg_rplan_create(int64_t N, const int64_t* indptr, const int32_t* indices, int64_t nnz_full,
+                                int64_t n_solve, const int64_t* solve_ids, void* stream, emg_rplan** out) {
+    using namespace emg;
+    EMG_CHECK_ARG(out && indptr && indices && (solve_ids || n_solve == 0), "emg_rplan_create: NULL argument");
+    EMG_CHECK_ARG(N >= 0 && n_solve >= 0 && n_solve <= N, "emg_rplan_create: bad size");
+    cudaStream_t s = (cudaStream_t)stream;
+    emg_rplan* p = new emg_rplan();
+    p->N = N;
+    p->ns = n_solve;
+    p->nnz_full = nnz_full;
+    const int64_t ns = n_solve;
+    int64_t* cnt = nullptr;
+    int64_t* tmp = nullptr;
+    auto fail = [&](int code) { dfree(cnt); dfree(tmp); rplan_free(p); return code; };
+#define TRY(x) do { int _r = (x); if (_r) return fail(_r); } while (0)
+#define TRYC(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) return fail(cuda_status(_e, #x)); } while (0)
+    TRY(dalloc(&p->sid, ns + 1, "solve ids"));
+    TRY(dalloc(&p->map, N + 1, "dof map"));
+    TRY(dalloc(&p->rptr, ns + 1, "restricted indptr"));
+    TRY(dalloc(&p->rdiag, ns + 1, "restricted diag"));
+    TRY(dalloc(&cnt, ns + 1, "row counts"));
+    TRY(dalloc(&tmp, scan_scratch_elems(ns + 1) + 1, "scan scratch"));
+    if (ns > 0) TRYC(cudaMemcpyAsync(p->sid, solve_ids, sizeof(int64_t) * ns, cudaMemcpyDeviceToDevice, s));
+    if (N > 0) TRYC(cudaMemsetAsync(p->map, 0xff, sizeof(int32_t) * N, s));
+    const int T = 256;
+    if (ns > 0) {
+        kry::k_map<<<grid_for(ns, T), T, 0, s>>>(ns, p->sid, p->map);
+        kry::k_rcount<<<grid_for(ns, T), T, 0, s>>>(ns, p->sid, indptr, indices, p->map, cnt);
+        TRYC(cudaGetLastError());
+    }
+    TRY(scan_exclusive_i64(cnt, p->rptr, ns, tmp, s));
+    TRYC(cudaMemcpyAsync(&p->nnz, p->rptr + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    TRYC(cudaStreamSynchronize(s));
+    TRY(dalloc(&p->rind, p->nnz + 1, "restricted indices"));
+    TRY(dalloc(&p->rsrc, p->nnz + 1, "restricted sources"));
+    if (ns > 0) {
+        kry::k_rwrite<<<grid_for(ns, T), T, 0, s>>>(ns, p->sid, indptr, indices, p->map, p->rptr, p->rind, p->rsrc,
+                                                    p->rdiag);
+        TRYC(cudaGetLastError());
+    }
+    // host: levels and factorization update lists
+    std::vector<int64_t> rptr(ns + 1), rdiag(ns);
+    std::vector<int32_t> rind(p->nnz);
+    TRYC(cudaMemcpyAsync(rptr.data(), p->rptr, sizeof(int64_t) * (ns + 1), cudaMemcpyDeviceToHost, s));
+    if (ns > 0) TRYC(cudaMemcpyAsync(rdiag.data(), p->rdiag, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, s));
+    if (p->nnz > 0) TRYC(cudaMemcpyAsync(rind.data(), p->rind, sizeof(int32_t) * p->nnz, cudaMemcpyDeviceToHost, s));
+    TRYC(cudaStreamSynchronize(s));
+    for (int64_t i = 0; i < ns; ++i)
+        if (rdiag[i] < 0) {
+            set_error("emg_rplan_create: restricted row " + std::to_string(i) + " has no diagonal entry");
+            return fail(EMG_ERR_MESH);
+        }
+    std::vector<int32_t> lev(ns, 0), ulev(ns, 0);
+    int32_t nl = 0, nu = 0;
+    for (int64_t i = 0; i < ns; ++i) {
+        int32_t l = 0;
+        for (int64_t k = rptr[i]; k < rdiag[i]; ++k) l = std::max(l, lev[rind[k]] + 1);
+        lev[i] = l;
+        nl = std::max(nl, l + 1);
+    }
+    for (int64_t i = ns - 1; i >= 0; --i) {
+        int32_t l = 0;
+        for (int64_t k = rdiag[i] + 1; k < rptr[i + 1]; ++k) l = std::max(l, ulev[rind[k]] + 1);
+        ulev[i] = l;
+        nu = std::max(nu, l + 1);
+    }
+    auto bucket = [&](const std::vector<int32_t>& lv, int32_t nlev, std::vector<int64_t>& ptr, std::vector<int32_t>& rows) {
+        ptr.assign(nlev + 1, 0);
+        for (int64_t i = 0; i < ns; ++i) ptr[lv[i] + 1]++;
+        for (int32_t l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+        rows.resize(ns);
+        std::vector<int64_t> pos(ptr.begin(), ptr.end() - 1);
+        for (int64_t i = 0; i < ns; ++i) rows[pos[lv[i]]++] = (int32_t)i;
+    };
+    std::vector<int32_t> lrows, urows;
+    bucket(lev, nl, p->lptr, lrows);
+    bucket(ulev, nu, p->uptr_lv, urows);
+    // update lists: for row i, each kk in its L part (column k), each entry of row k's U
+    // part whose column is in row i: (kk local index << 32 | source pos, target pos)
+    std::vector<int64_t> uptr(ns + 1, 0), ulist;
+    ulist.reserve((size_t)p->nnz * 8);
+    std::vector<int64_t> where(ns, -1);
+    for (int64_t i = 0; i < ns; ++i) {
+        for (int64_t k = rptr[i]; k < rptr[i + 1]; ++k) where[rind[k]] = k;
+        for (int64_t kk = rptr[i]; kk < rdiag[i]; ++kk) {
+            const int32_t k = rind[kk];
+            for (int64_t jj = rdiag[k] + 1; jj < rptr[k + 1]; ++jj) {
+                const int64_t t = where[rind[jj]];
+                if (t < 0) continue;
+                ulist.push_back(((kk - rptr[i]) << 32) | jj);
+                ulist.push_back(t);
+            }
+        }
+        for (int64_t k = rptr[i]; k < rptr[i + 1]; ++k) where[rind[k]] = -1;
+        uptr[i + 1] = (int64_t)ulist.size() / 2;
+    }
+    TRY(dalloc(&p->uptr, ns + 1, "ilu update ptr"));
+    TRY(dalloc(&p->ulist, (int64_t)ulist.size() + 2, "ilu update list"));
+    TRY(dalloc(&p->lrows, ns + 1, "L level rows"));
+    TRY(dalloc(&p->urows, ns + 1, "U level rows"));
+    TRYC(cudaMemcpyAsync(p->uptr, uptr.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, s));
+    if (!ulist.empty())
+        TRYC(cudaMemcpyAsync(p->ulist, ulist.data(), sizeof(int64_t) * ulist.size(), cudaMemcpyHostToDevice, s));
+    if (ns > 0) {
+        TRYC(cudaMemcpyAsync(p->lrows, lrows.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, s));
+        TRYC(cudaMemcpyAsync(p->urows, urows.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, s));
+    }
+    TRYC(cudaStreamSynchronize(s));
+    TRYC(cudaStreamCreateWithFlags(&p->gs, cudaStreamNonBlocking));
+    TRYC(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
+    TRYC(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming));
+    dfree(cnt);
+    dfree(tmp);
+#undef TRY
+#undef TRYC
+    *out = p;
+    return EMG_OK;
+}
+
+extern "C" int64_t emg_rplan_n(const emg_rplan* p) { return p ? p->ns : -1; }
+extern "C" int64_t emg_rplan_nnz(const emg_rplan* p) { return p ? p->nnz : -1; }
+extern "C" int64_t emg_rplan_levels(const emg_rplan* p) { return p ? (int64_t)p->lptr.size() - 1 : -1; }
+extern "C" void emg_rplan_destroy(emg_rplan* p) { rplan_free(p); }
+
+extern "C" int emg_rplan_form(const emg_rplan* p, int64_t Bm, const double* E, const double* B, const double* k2,
+                              int64_t n_ports, const double* P, const double* gam, double* A, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p && E && B && k2 && A && Bm > 0 && n_ports >= 0 && (n_ports == 0 || (P && gam)),
+                  "emg_rplan_form: bad argument");
+    if (p->nnz == 0) return EMG_OK;
+    kry::k_form<<<grid_for(p->nnz * Bm, 256), 256, 0, (cudaStream_t)stream>>>(
+        p->nnz, Bm, p->rsrc, reinterpret_cast<const double2*>(E), reinterpret_cast<const double2*>(B), k2, n_ports,
+        reinterpret_cast<const double2*>(P), p->nnz_full, reinterpret_cast<const double2*>(gam),
+        reinterpret_cast<double2*>(A));
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+
+extern "C" int emg_ilu0(const emg_rplan* p, int64_t Bm, double* LU, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p && LU && Bm > 0, "emg_ilu0: bad argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    for (size_t l = 0; l + 1 < p->lptr.size(); ++l) {
+        const int64_t r0 = p->lptr[l], nr = p->lptr[l + 1] - r0;
+        kry::k_ilu_level<<<grid_for(nr * Bm, 128), 128, 0, s>>>(nr, p->lrows + r0, Bm, p->rptr, p->rind, p->rdiag,
+                                                                p->uptr, p->ulist, reinterpret_cast<double2*>(LU));
+    }
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+
+namespace {
+int trsv(const emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double2* LU, double2* X, cudaStream_t s) {
+    for (size_t l = 0; l + 1 < p->lptr.size(); ++l) {
+        const int64_t r0 = p->lptr[l], nr = p->lptr[l + 1] - r0;
+        kry::k_trsv_level<<<grid_for(nr * Bc, 128), 128, 0, s>>>(nr, p->lrows + r0, Bc, cmat, Bm, p->rptr, p->rind,
+                                                                 p->rdiag, LU, 0, X);
+    }
+    for (size_t l = 0; l + 1 < p->uptr_lv.size(); ++l) {
+        const int64_t r0 = p->uptr_lv[l], nr = p->uptr_lv[l + 1] - r0;
+        kry::k_trsv_level<<<grid_for(nr * Bc, 128), 128, 0, s>>>(nr, p->urows + r0, Bc, cmat, Bm, p->rptr, p->rind,
+                                                                 p->rdiag, LU, 1, X);
+    }
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+}  // namespace
+
+extern "C" int emg_ilu_apply(const emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* LU,
+                             double* X, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p && cmat && LU && X && Bc > 0 && Bm > 0, "emg_ilu_apply: bad argument");
+    return trsv(p, Bc, cmat, Bm, reinterpret_cast<const double2*>(LU), reinterpret_cast<double2*>(X),
+                (cudaStream_t)stream);
+}
+
+extern "C" int emg_spmv(const emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A,
+                        const double* X, const double* Bv, double* Y, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p && cmat && A && X && Y && Bc > 0 && Bm > 0, "emg_spmv: bad argument");
+    if (p->ns == 0) return EMG_OK;
+    kry::k_spmv<<<grid_for(p->ns * Bc, 256), 256, 0, (cudaStream_t)stream>>>(
+        p->ns, Bc, cmat, Bm, p->rptr, p->rind, reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(X),
+        reinterpret_cast<const double2*>(Bv), reinterpret_cast<double2*>(Y));
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+
+extern "C" int emg_rplan_gather(const emg_rplan* p, int64_t Bc, const double* full, double* out, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p && full && out && Bc > 0, "emg_rplan_gather: bad argument");
+    if (p->ns == 0) return EMG_OK;
+    kry::k_gather_rhs<<<grid_for(p->ns * Bc, 256), 256, 0, (cudaStream_t)stream>>>(
+        p->ns, Bc, p->sid, p->N, reinterpret_cast<const double2*>(full), reinterpret_cast<double2*>(out));
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+
+extern "C" int emg_rplan_scatter(const emg_rplan* p, int64_t Bc, const double* x, double* full, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p && x && full && Bc > 0, "emg_rplan_scatter: bad argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    EMG_CUDA(cudaMemsetAsync(full, 0, sizeof(double) * 2 * p->N * Bc, s));
+    if (p->ns == 0) return EMG_OK;
+    kry::k_scatter_sol<<<grid_for(p->ns * Bc, 256), 256, 0, s>>>(p->ns, Bc, p->sid, p->N,
+                                                                reinterpret_cast<const double2*>(x),
+                                                                reinterpret_cast<double2*>(full));
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+
+// ------------------------------------------------------------------ GMRES ---
+// Right-preconditioned restarted GMRES(m) with classical Gram-Schmidt applied
+// twice (CGS2), all columns in lockstep; a column stops updating once its
+// implicit residual reaches tol * ||b||.  The final residual is recomputed
+// explicitly in FP64 (resid_out) after every restart.
+namespace {
+void dots(int64_t n, int64_t Bc, int nj, const double2* V, int64_t vstride, const double2* W, double2* part,
+          int64_t nblk, cudaStream_t s) {
+    if (Bc < 32) {
+        kry::k_dots_partial_small<<<(unsigned)nblk, 256, 0, s>>>(n, Bc, nj, V, vstride, W, part);
+    } else {
+        const dim3 g((unsigned)nblk, (unsigned)((Bc + 127) / 128));
+        kry::k_dots_partial<<<g, 128, 0, s>>>(n, Bc, nj, V, vstride, W, part);
+    }
+}
+}  // namespace
+
+extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A_,
+                         const double* LU_, const double* rhs_, double* x_, int restart, int max_iter, double tol,
+                         int32_t* iters_out, double* resid_out, void* stream) {
+    using namespace emg;
+    emg_rplan* p = const_cast<emg_rplan*>(pc);
+    EMG_CHECK_ARG(p && cmat && A_ && LU_ && rhs_ && x_ && iters_out && resid_out && Bc > 0 && Bm > 0,
+                  "emg_gmres: bad argument");
+    EMG_CHECK_ARG(restart >= 1 && restart <= kry::kMaxRestart && max_iter >= 1 && tol > 0,
+                  "emg_gmres: restart must be in [1, 256]");
+    cudaStream_t caller = (cudaStream_t)stream;
+    const int64_t n = p->ns;
+    if (n == 0) return EMG_OK;
+    EMG_CUDA(cudaEventRecord(p->ev_in, caller));
+    EMG_CUDA(cudaStreamWaitEvent(p->gs, p->ev_in, 0));
+    cudaStream_t s = p->gs;
+    const int m = restart;
+    const auto* A = reinterpret_cast<const double2*>(A_);
+    const auto* LU = reinterpret_cast<const double2*>(LU_);
+    const auto* rhs = reinterpret_cast<const double2*>(rhs_);
+    auto* x = reinterpret_cast<double2*>(x_);
+    const int64_t vec = n * Bc;
+    const int64_t nblk = (n + kry::kDotRows - 1) / kry::kDotRows;
+    // workspace layout
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
+    const size_t oV = take(sizeof(double2) * vec * (m + 1));
+    const size_t oW = take(sizeof(double2) * vec);
+    const size_t oT = take(sizeof(double2) * vec);
+    const size_t oPart = take(sizeof(double2) * nblk * (m + 1) * Bc);
+    const size_t oH1 = take(sizeof(double2) * (m + 1) * Bc);
+    const size_t oH2 = take(sizeof(double2) * (m + 1) * Bc);
+    const size_t oH = take(sizeof(double2) * m * m * Bc);
+    const size_t oCs = take(sizeof(double2) * m * Bc);
+    const size_t oSn = take(sizeof(double2) * m * Bc);
+    const size_t oG = take(sizeof(double2) * (m + 1) * Bc);
+    const size_t oY = take(sizeof(double2) * m * Bc);
+    const size_t oBn = take(sizeof(double) * Bc);
+    const size_t oVs = take(sizeof(double) * Bc);
+    const size_t oWn = take(sizeof(double) * Bc);
+    const size_t oAct = take(sizeof(int32_t) * Bc);
+    const size_t oLen = take(sizeof(int32_t) * Bc);
+    const size_t oRes = take(sizeof(double) * Bc);
+    const size_t oIt = take(sizeof(int32_t) * Bc);
+    if (off > p->ws_bytes) {
+        if (p->ws) cudaFree(p->ws);
+        p->ws = nullptr;
+        p->ws_bytes = 0;
+        EMG_CUDA(cudaMalloc(&p->ws, off));
+        p->ws_bytes = off;
+    }
+    char* base = static_cast<char*>(p->ws);
+    auto* V = reinterpret_cast<double2*>(base + oV);
+    auto* W = reinterpret_cast<double2*>(base + oW);
+    auto* Tv = reinterpret_cast<double2*>(base + oT);
+    auto* part = reinterpret_cast<double2*>(base + oPart);
+    auto* h1 = reinterpret_cast<double2*>(base + oH1);
+    auto* h2 = reinterpret_cast<double2*>(base + oH2);
+    auto* H = reinterpret_cast<double2*>(base + oH);
+    auto* cs = reinterpret_cast<double2*>(base + oCs);
+    auto* sn = reinterpret_cast<double2*>(base + oSn);
+    auto* g = reinterpret_cast<double2*>(base + oG);
+    auto* y = reinterpret_cast<double2*>(base + oY);
+    auto* bn = reinterpret_cast<double*>(base + oBn);
+    auto* vs = reinterpret_cast<double*>(base + oVs);
+    auto* wn = reinterpret_cast<double*>(base + oWn);
+    auto* act = reinterpret_cast<int32_t*>(base + oAct);
+    auto* len = reinterpret_cast<int32_t*>(base + oLen);
+    auto* res = reinterpret_cast<double*>(base + oRes);
+    auto* its = reinterpret_cast<int32_t*>(base + oIt);
+    const int T = 256;
+    const dim3 dgrid((unsigned)nblk, (unsigned)((Bc + 127) / 128));
+    const unsigned cgrid = (unsigned)((Bc + 127) / 128);
+    auto norms2 = [&](const double2* Vv) {   // h1[c] = ||Vv[:,c]||^2 (real part)
+        dots(n, Bc, 1, Vv, vec, Vv, part, nblk, s);
+        kry::k_dots_final<<<cgrid, 128, 0, s>>>(nblk, Bc, 1, part, h1);
+        return h1;
+    };
+    kry::k_sqrt_real<<<cgrid, 128, 0, s>>>(Bc, norms2(rhs), bn);
+    EMG_CUDA(cudaMemsetAsync(its, 0, sizeof(int32_t) * Bc, s));
+    // one Arnoldi step for Krylov index j (captured once per j into a CUDA graph)
+    auto step = [&](int j) -> int {
+        double2* Vj = V + (int64_t)j * vec;
+        EMG_CUDA(cudaMemcpyAsync(Tv, Vj, sizeof(double2) * vec, cudaMemcpyDeviceToDevice, s));
+        int rc = trsv(p, Bc, cmat, Bm, LU, Tv, s);
+        if (rc) return rc;
+        kry::k_spmv<<<grid_for(vec, T), T, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, Tv, nullptr, W);
+        // CGS2: two passes of h = V^H w, w -= V h
+        const unsigned hgrid = (unsigned)(((int64_t)(j + 1) * Bc + 127) / 128);
+        dots(n, Bc, j + 1, V, vec, W, part, nblk, s);
+        kry::k_dots_final<<<hgrid, 128, 0, s>>>(nblk, Bc, j + 1, part, h1);
+        kry::k_orth_update<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j + 1, V, vec, h1, act, W);
+        dots(n, Bc, j + 1, V, vec, W, part, nblk, s);
+        kry::k_dots_final<<<hgrid, 128, 0, s>>>(nblk, Bc, j + 1, part, h2);
+        kry::k_orth_update<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j + 1, V, vec, h2, act, W);
+        dots(n, Bc, 1, W, vec, W, part, nblk, s);
+        kry::k_dots_final<<<cgrid, 128, 0, s>>>(nblk, Bc, 1, part, y);
+        kry::k_real<<<cgrid, 128, 0, s>>>(Bc, y, wn);
+        kry::k_arnoldi_col<<<cgrid, 128, 0, s>>>(Bc, j, m, h1, h2, wn, H, cs, sn, g, bn, tol, act, len, vs, res);
+        kry::k_scale_cols<<<grid_for(vec, T), T, 0, s>>>(n, Bc, vs, W, V + (int64_t)(j + 1) * vec);
+        EMG_CUDA(cudaGetLastError());
+        return EMG_OK;
+    };
+    std::vector<cudaGraphExec_t> graphs(m, nullptr);
+    struct GraphGuard {
+        std::vector<cudaGraphExec_t>* g;
+        ~GraphGuard() { for (auto& e : *g) if (e) cudaGraphExecDestroy(e); }
+    } guard{&graphs};
+    int total = 0;
+    std::vector<int32_t> hact(Bc), hprev(Bc), hits(Bc, 0);
+    while (total < max_iter) {
+        // r = b - A x ; V0 = r / ||r||
+        kry::k_spmv<<<grid_for(vec, T), T, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, x, rhs, W);
+        double2* rr = norms2(W);
+        kry::k_restart_cols<<<cgrid, 128, 0, s>>>(Bc, rr, bn, tol, g, vs, act, len, res, m + 1);
+        kry::k_scale_cols<<<grid_for(vec, T), T, 0, s>>>(n, Bc, vs, W, V);
+        EMG_CUDA(cudaGetLastError());
+        EMG_CUDA(cudaMemcpyAsync(hact.data(), act, sizeof(int32_t) * Bc, cudaMemcpyDeviceToHost, s));
+        EMG_CUDA(cudaStreamSynchronize(s));
+        bool any = false;
+        for (int64_t c = 0; c < Bc; ++c) any |= hact[c] != 0;
+        if (!any) break;
+        int j = 0;
+        while (j < m && total < max_iter) {
+            if (!graphs[j]) {
+                cudaGraph_t gr = nullptr;
+                EMG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                const int rc = step(j);
+                const cudaError_t ec = cudaStreamEndCapture(s, &gr);
+                if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+                if (ec != cudaSuccess) return cuda_status(ec, "cudaStreamEndCapture");
+                const cudaError_t ei = cudaGraphInstantiate(&graphs[j], gr, 0);
+                cudaGraphDestroy(gr);
+                if (ei != cudaSuccess) return cuda_status(ei, "cudaGraphInstantiate");
+            }
+            hprev = hact;
+            EMG_CUDA(cudaGraphLaunch(graphs[j], s));
+            ++j;
+            ++total;
+            EMG_CUDA(cudaMemcpyAsync(hact.data(), act, sizeof(int32_t) * Bc, cudaMemcpyDeviceToHost, s));
+            EMG_CUDA(cudaStreamSynchronize(s));
+            bool any2 = false;
+            for (int64_t c = 0; c < Bc; ++c) {
+                if (hprev[c]) hits[c] = total;
+                any2 |= hact[c] != 0;
+            }
+            if (!any2) break;
+        }
+        // x += M^-1 (V y)   (y from back substitution over each column's Krylov length)
+        kry::k_backsolve<<<cgrid, 128, 0, s>>>(Bc, m, H, g, len, y, j);
+        EMG_CUDA(cudaMemsetAsync(Tv, 0, sizeof(double2) * vec, s));
+        kry::k_combine_basis<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j, V, vec, y, Tv);
+        {
+            int rc = trsv(p, Bc, cmat, Bm, LU, Tv, s);
+            if (rc) return rc;
+        }
+        kry::k_axpy1<<<grid_for(vec, T), T, 0, s>>>(vec, Tv, x);
+        EMG_CUDA(cudaGetLastError());
+    }
+    // explicit final residual
+    kry::k_spmv<<<grid_for(vec, T), T, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, x, rhs, W);
+    double2* rr = norms2(W);
+    std::vector<double2> hr(Bc);
+    std::vector<double> hb(Bc), hres(Bc);
+    EMG_CUDA(cudaMemcpyAsync(hr.data(), rr, sizeof(double2) * Bc, cudaMemcpyDeviceToHost, s));
+    EMG_CUDA(cudaMemcpyAsync(hb.data(), bn, sizeof(double) * Bc, cudaMemcpyDeviceToHost, s));
+    EMG_CUDA(cudaStreamSynchronize(s));
+    for (int64_t c = 0; c < Bc; ++c) hres[c] = hb[c] > 0 ? sqrt(std::max(hr[c].x, 0.0)) / hb[c] : 0.0;
+    EMG_CUDA(cudaMemcpyAsync(resid_out, hres.data(), sizeof(double) * Bc, cudaMemcpyHostToDevice, s));
+    EMG_CUDA(cudaMemcpyAsync(iters_out, hits.data(), sizeof(int32_t) * Bc, cudaMemcpyHostToDevice, s));
+    EMG_CUDA(cudaStreamSynchronize(s));
+    EMG_CUDA(cudaEventRecord(p->ev_out, s));
+    EMG_CUDA(cudaStreamWaitEvent(caller, p->ev_out, 0));
+    return EMG_OK;
+}

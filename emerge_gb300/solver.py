@@ -1,0 +1,406 @@
+"""GPU linear solves of the frequency-domain system.
+
+* ``RestrictedSystem`` — the PEC-restricted pattern ``A[ix_(solve_ids, solve_ids)]``
+  (fem/solver.py:434-435) with its ILU(0) schedule, built once per (mesh, PEC set).
+* ``GPUSolver`` — drop-in for the ``direct_solver`` slot of the reference
+  ``SolveRoutine`` (fem/solver.py:117-131, 405-469): ``solve(A, b, precon,
+  reuse_factorization) -> (x, info)``; ILU(0)-preconditioned GMRES in FP64 on the
+  GPU, info as in SciPy (0 converged, > 0 iterations without convergence).
+* ``FrequencySweep`` — a whole ``frequency_domain`` sweep
+  (fem/physics/edm/emfreq3d.py:607-732) with the matrices, the solves and the
+  S-parameters resident on the GPU: ``plain`` solves one frequency at a time,
+  ``batched`` solves every (frequency, port) column in lockstep, optionally from
+  a warm start.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .bc import C0, is_port
+
+
+def _vp(t) -> ctypes.c_void_p:
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def _stream() -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class RestrictedSystem:
+    """PEC-restricted CSR pattern + ILU(0) structure (emg_rplan)."""
+
+    def __init__(self, indptr: torch.Tensor, indices: torch.Tensor, nnz_full: int, solve_ids: np.ndarray):
+        self.device = indptr.device
+        self.N = int(indptr.numel() - 1)
+        self.nnz_full = int(nnz_full)
+        sid = torch.as_tensor(np.ascontiguousarray(solve_ids, dtype=np.int64), device=self.device)
+        plan = ctypes.c_void_p()
+        _lib.call("emg_rplan_create", self.N, _vp(indptr), _vp(indices), self.nnz_full, int(sid.numel()), _vp(sid),
+                  _stream(), ctypes.byref(plan))
+        self._plan = plan
+        self._lib = _lib.load()
+        self.n = int(self._lib.emg_rplan_n(plan))
+        self.nnz = int(self._lib.emg_rplan_nnz(plan))
+        self.levels = int(self._lib.emg_rplan_levels(plan))
+        self.solve_ids = np.asarray(solve_ids, dtype=np.int64)
+
+    def __del__(self):
+        p = getattr(self, "_plan", None)
+        if p is not None and p.value:
+            try:
+                self._lib.emg_rplan_destroy(p)
+            except Exception:
+                pass
+            self._plan = None
+
+    def form(self, E, B, k2, P=None, gam=None) -> torch.Tensor:
+        """Bm restricted matrices (nnz_r, Bm): E - k2[m] B + sum_p gam[p, m] P[p]."""
+        k2 = torch.as_tensor(np.ascontiguousarray(k2, dtype=np.float64), device=self.device)
+        Bm = int(k2.numel())
+        n_ports = 0 if P is None else int(P.shape[0])
+        if n_ports:
+            gam = torch.as_tensor(np.ascontiguousarray(gam, dtype=np.complex128), device=self.device)
+        A = torch.empty((max(self.nnz, 1), Bm), dtype=torch.complex128, device=self.device)
+        _lib.call("emg_rplan_form", self._plan, Bm, _vp(E), _vp(B), _vp(k2), n_ports, _vp(P) if n_ports else None,
+                  _vp(gam) if n_ports else None, _vp(A), _stream())
+        return A
+
+    def ilu0(self, A: torch.Tensor) -> torch.Tensor:
+        LU = A.contiguous().clone()
+        _lib.call("emg_ilu0", self._plan, int(A.shape[1]), _vp(LU), _stream())
+        return LU
+
+    def gather(self, full: torch.Tensor) -> torch.Tensor:
+        """full (Bc, N) -> restricted (n, Bc)."""
+        Bc = int(full.shape[0])
+        out = torch.empty((self.n, Bc), dtype=torch.complex128, device=self.device)
+        _lib.call("emg_rplan_gather", self._plan, Bc, _vp(full.contiguous()), _vp(out), _stream())
+        return out
+
+    def scatter(self, x: torch.Tensor) -> torch.Tensor:
+        """restricted (n, Bc) -> full (Bc, N), zeros on removed DOFs."""
+        Bc = int(x.shape[1])
+        full = torch.empty((Bc, self.N), dtype=torch.complex128, device=self.device)
+        _lib.call("emg_rplan_scatter", self._plan, Bc, _vp(x.contiguous()), _vp(full), _stream())
+        return full
+
+    def spmv(self, A, X, cmat, Bv=None) -> torch.Tensor:
+        X = X.contiguous()
+        A = A.contiguous()
+        Bv = None if Bv is None else Bv.contiguous()
+        Y = torch.empty(X.shape, dtype=X.dtype, device=X.device)
+        _lib.call("emg_spmv", self._plan, int(X.shape[1]), _vp(cmat), int(A.shape[1]), _vp(A), _vp(X),
+                  _vp(Bv) if Bv is not None else None, _vp(Y), _stream())
+        return Y
+
+    def gmres(self, A, LU, rhs, cmat, x0=None, restart=150, max_iter=20000, tol=1e-10):
+        """Solve column c of rhs (n, Bc) with matrix cmat[c]; returns (x, iters, resid)."""
+        Bc = int(rhs.shape[1])
+        rhs = rhs.contiguous()
+        A = A.contiguous()
+        LU = LU.contiguous()
+        x = torch.zeros(rhs.shape, dtype=rhs.dtype, device=rhs.device) if x0 is None else x0.contiguous().clone()
+        its = torch.zeros(Bc, dtype=torch.int32, device=self.device)
+        res = torch.zeros(Bc, dtype=torch.float64, device=self.device)
+        _lib.call("emg_gmres", self._plan, Bc, _vp(cmat), int(A.shape[1]), _vp(A), _vp(LU), _vp(rhs.contiguous()),
+                  _vp(x), int(restart), int(max_iter), ctypes.c_double(tol), _vp(its), _vp(res), _stream())
+        return x, its.cpu().numpy(), res.cpu().numpy()
+
+
+class GPUSolver:
+    """``Solver`` for the reference SolveRoutine (fem/solver.py:117-131): GPU ILU(0)-GMRES.
+
+    ``A`` arrives restricted (CSC/CSR, complex), ``b`` restricted.  The pattern
+    analysis is cached across calls with the same pattern (every frequency of a
+    sweep); with ``reuse_factorization`` the previous ILU factors are reused
+    (the second port of the same frequency, emfreq3d.py:686-697).
+    """
+
+    real_only = False
+    req_sorter = False
+
+    def __init__(self, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000, device="cuda"):
+        self.own_preconditioner = True
+        self.tol = tol
+        self.restart = restart
+        self.max_iter = max_iter
+        self.device = torch.device(device)
+        self._key = None
+        self._sys = None
+        self._A = None
+        self._LU = None
+        self.last_iterations = 0
+        self.last_residual = 0.0
+
+    def __str__(self):
+        return "GPUSolver"
+
+    def solve(self, A, b, precon=None, reuse_factorization: bool = False):
+        from scipy.sparse import csr_matrix
+        A = csr_matrix(A)
+        A.sort_indices()
+        n = A.shape[0]
+        key = (n, A.nnz, hash(A.indices[: min(A.nnz, 4096)].tobytes()), hash(A.indptr.tobytes()))
+        dev = self.device
+        if key != self._key:
+            indptr = torch.as_tensor(A.indptr.astype(np.int64), device=dev)
+            indices = torch.as_tensor(A.indices.astype(np.int32), device=dev)
+            self._sys = RestrictedSystem(indptr, indices, A.nnz, np.arange(n))
+            self._key = key
+            reuse_factorization = False
+        sysr = self._sys
+        vals = torch.as_tensor(A.data.astype(np.complex128), device=dev)
+        zeros = torch.zeros_like(vals)
+        if not reuse_factorization or self._LU is None:
+            self._A = sysr.form(vals, zeros, [0.0])
+            self._LU = sysr.ilu0(self._A)
+        rhs = torch.as_tensor(np.asarray(b, dtype=np.complex128), device=dev).reshape(1, n)
+        r = sysr.gather(rhs)
+        cmat = torch.zeros(1, dtype=torch.int32, device=dev)
+        x, its, res = sysr.gmres(self._A, self._LU, r, cmat, restart=self.restart, max_iter=self.max_iter, tol=self.tol)
+        self.last_iterations = int(its[0])
+        self.last_residual = float(res[0])
+        info = 0 if res[0] <= self.tol * 10 else int(its[0])
+        return sysr.scatter(x)[0].cpu().numpy(), info
+
+
+# ------------------------------------------------------------------ sweep ---
+@dataclass
+class SweepResult:
+    freqs: np.ndarray
+    S: np.ndarray                     # (nf, np, np) complex
+    iterations: np.ndarray            # (nf, np)
+    residuals: np.ndarray             # (nf, np) explicit relative residuals
+    seconds: float                    # wall time of the solve phase
+    solutions: torch.Tensor | None = None   # (n, nf*np) restricted solutions (device)
+    info: dict = field(default_factory=dict)
+
+
+class FrequencySweep:
+    """Frequency sweep of ``Electrodynamics3D.frequency_domain`` on the GPU.
+
+    Args:
+        assembler: an ``emerge_gb300.freq.Assembler`` (volume E, B cached on it).
+        field, er, ur, bcs: as for ``Assembler.assemble_freq_matrix``.
+
+    Port matrices are linear in gamma (Robin blocks, fem/mth/tri.py:630,694), so
+    A(k) = E - k^2 B + sum_p gamma_p(k) P_p with unit matrices P_p built once;
+    port right-hand sides are linear in beta (U_inc = -2j beta E_mode,
+    fem/bc.py:588-589), b_p(k) = -2j beta_p(k) u_p with u_p = int N . E_mode.
+    S-parameters use the same quadrature as fem/mth/sparam.py:102-139:
+    S_ij = (-x_j . u_i - delta_ij P_i) / P_i, P_i = int |E_mode_i|^2, since the
+    forcing entries are u_i = -int N . E_mode_i.
+    """
+
+    def __init__(self, assembler, field, er, ur, bcs):
+        self.asm = assembler
+        self.field = field
+        self.bcs = bcs
+        self.ports = sorted([bc for bc in bcs if is_port(bc)], key=lambda b: b.port_number)
+        dev = assembler.device
+        self.device = dev
+        plan, E, B = assembler._volume(field, er, ur)
+        self.plan, self.E, self.B = plan, E, B
+        N = plan.n_field
+        # unit port matrices (gamma = 1) and unit forcing vectors (U_inc = E_mode)
+        unit_bcs = []
+        for bc in bcs:
+            unit_bcs.append(_UnitRobin(bc) if hasattr(bc, "get_gamma") and hasattr(bc, "_include_stiff") else bc)
+        robin = [u for u in unit_bcs if isinstance(u, _UnitRobin)]
+        self.robin = robin
+        sysd = assembler.device_system(field, er, ur, unit_bcs, frequency=C0 / (2 * np.pi))   # k0 = 1
+        # per Robin BC: its unit matrix alone = K(unit only) - (E - B); build each separately
+        P = torch.zeros((len(robin), plan.nnz), dtype=torch.complex128, device=dev)
+        for i, u in enumerate(robin):
+            solo = [b for b in unit_bcs if not isinstance(b, _UnitRobin)] + [u]
+            s1 = assembler.device_system(field, er, ur, solo, frequency=C0 / (2 * np.pi))
+            P[i] = s1.K - (E - B)
+        self.P = P
+        self.u = {bc.port_number: sysd.port_vectors[bc.port_number] for bc in self.ports}
+        self.solve_ids = sysd.solve_ids
+        self.sys = RestrictedSystem(plan.indptr, plan.indices[: plan.nnz], plan.nnz, self.solve_ids)
+        self.u_r = self.sys.gather(torch.stack([self.u[bc.port_number] for bc in self.ports]))   # (n, np)
+        self.Pmode = np.array([_mode_power(field, bc) for bc in self.ports])
+
+    def _coeffs(self, freqs):
+        k0 = 2 * np.pi * np.asarray(freqs, dtype=float) / C0
+        gam = np.array([[complex(u.bc.get_gamma(k)) for k in k0] for u in self.robin]).reshape(len(self.robin), len(k0))
+        beta = np.array([[complex(bc.get_beta(k)) for k in k0] for bc in self.ports])     # (np, nf)
+        return k0, gam, beta
+
+    def _rhs(self, beta):
+        """(n, nf*np) restricted right-hand sides, column f*np + p."""
+        nf = beta.shape[1]
+        npo = len(self.ports)
+        scale = torch.as_tensor((-2j * beta.T).reshape(-1), device=self.device)                  # (nf*np)
+        cols = self.u_r[:, torch.arange(npo, device=self.device).repeat(nf)]                    # (n, nf*np)
+        return cols * scale[None, :]
+
+    def _sparams(self, X, nf, beta):
+        npo = len(self.ports)
+        # int E_c . E_mode_i = -x_c . u_i: the waveport forcing of fem/mth/tri.py:668-693
+        # is -int N . U_inc (its signA * Area factor), so u_i = -int N . E_mode_i
+        # (E_mode real: no conjugation)
+        G = -(self.u_r.T @ X).cpu().numpy()                                                      # (np, nf*np)
+        S = np.zeros((nf, npo, npo), dtype=np.complex128)
+        for f in range(nf):
+            for j in range(npo):
+                for i in range(npo):
+                    S[f, i, j] = (G[i, f * npo + j] - (self.Pmode[i] if i == j else 0.0)) / self.Pmode[i]
+        return S
+
+    def run(self, freqs, method: str = "batched", tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
+            x0: torch.Tensor | None = None, chunk: int | None = None) -> SweepResult:
+        freqs = np.asarray(freqs, dtype=float)
+        nf, npo = len(freqs), len(self.ports)
+        k0, gam, beta = self._coeffs(freqs)
+        sysr = self.sys
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        X = torch.zeros((sysr.n, nf * npo), dtype=torch.complex128, device=self.device)
+        its = np.zeros(nf * npo, dtype=np.int64)
+        res = np.zeros(nf * npo)
+        if method == "plain":
+            for f in range(nf):
+                A = sysr.form(self.E, self.B, [k0[f] ** 2], self.P, gam[:, f:f + 1])
+                LU = sysr.ilu0(A)
+                rhs = self._rhs(beta[:, f:f + 1])
+                cmat = torch.zeros(npo, dtype=torch.int32, device=self.device)
+                x, it, rs = sysr.gmres(A, LU, rhs, cmat, restart=restart, max_iter=max_iter, tol=tol)
+                X[:, f * npo:(f + 1) * npo] = x
+                its[f * npo:(f + 1) * npo] = it
+                res[f * npo:(f + 1) * npo] = rs
+        else:
+            chunk = chunk or nf
+            for f0 in range(0, nf, chunk):
+                f1 = min(nf, f0 + chunk)
+                A = sysr.form(self.E, self.B, k0[f0:f1] ** 2, self.P, gam[:, f0:f1])
+                LU = sysr.ilu0(A)
+                rhs = self._rhs(beta[:, f0:f1])
+                cmat = torch.arange(f1 - f0, dtype=torch.int32, device=self.device).repeat_interleave(npo)
+                xin = None if x0 is None else x0[:, f0 * npo:f1 * npo]
+                x, it, rs = sysr.gmres(A, LU, rhs, cmat, x0=xin, restart=restart, max_iter=max_iter, tol=tol)
+                X[:, f0 * npo:f1 * npo] = x
+                its[f0 * npo:f1 * npo] = it
+                res[f0 * npo:f1 * npo] = rs
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        S = self._sparams(X, nf, beta)
+        return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X)
+
+
+    # ------------------------------------------------------------ warm start ---
+    def _restricted_parts(self):
+        """Restricted E, B and unit port matrices as single-matrix value arrays (nnz_r, 1)."""
+        if getattr(self, "_parts", None) is None:
+            z = torch.zeros_like(self.E)
+            Er = self.sys.form(self.E, z, [0.0])
+            Br = self.sys.form(z, self.B, [-1.0])
+            Pr = []
+            for i in range(self.P.shape[0]):
+                g = np.zeros((self.P.shape[0], 1), dtype=np.complex128)
+                g[i, 0] = 1.0
+                Pr.append(self.sys.form(z, z, [0.0], self.P, g))
+            self._parts = (Er, Br, Pr)
+        return self._parts
+
+    def project(self, Xs: torch.Tensor, freqs, ports=None) -> torch.Tensor:
+        """Minimal-residual initial guesses in span(Xs) for every (frequency, port) column.
+
+        With Z_a = (E, B, P_1, ...) Xs and alpha(k) = (1, -k^2, gamma_1(k), ...),
+        A(k) Xs = sum_a alpha_a Z_a, so the normal equations of
+        min ||A(k) Xs y - b(k)|| only need the small Gram blocks Z_a^H Z_b and
+        Z_a^H u_p, computed once.  Returns X0 (n, nf*np).
+        """
+        Q, _ = torch.linalg.qr(Xs)                       # orthonormal basis (n, r)
+        Q = Q.contiguous()                               # LAPACK order is column-major
+        Er, Br, Pr = self._restricted_parts()
+        r = Q.shape[1]
+        cm = torch.zeros(r, dtype=torch.int32, device=self.device)
+        Zs = [self.sys.spmv(Er, Q, cm), self.sys.spmv(Br, Q, cm)] + [self.sys.spmv(Pi, Q, cm) for Pi in Pr]
+        Zc = torch.stack(Zs)                              # (na, n, r)
+        na = Zc.shape[0]
+        Gab = torch.einsum("ani,bnj->abij", Zc.conj(), Zc)               # (na, na, r, r)
+        Hu = torch.einsum("ani,np->api", Zc.conj(), self.u_r)           # (na, np, r)
+        freqs = np.asarray(freqs, dtype=float)
+        k0, gam, beta = self._coeffs(freqs)
+        nf, npo = len(freqs), len(self.ports)
+        alpha = np.zeros((nf, na), dtype=np.complex128)
+        alpha[:, 0] = 1.0
+        alpha[:, 1] = -k0 ** 2
+        alpha[:, 2:] = gam.T
+        al = torch.as_tensor(alpha, device=self.device)                 # (nf, na)
+        G = torch.einsum("fa,fb,abij->fij", al.conj(), al, Gab)          # (nf, r, r)
+        h = torch.einsum("fa,api->fpi", al.conj(), Hu)                   # (nf, np, r)
+        bscale = torch.as_tensor(-2j * beta.T, device=self.device)       # (nf, np)
+        h = h * bscale[:, :, None]
+        # ridge-free solve; G is Hermitian positive definite on a full-rank basis
+        y = torch.linalg.solve(G[:, None, :, :].expand(nf, npo, r, r), h[..., None])[..., 0]   # (nf, np, r)
+        X0 = Q @ y.reshape(nf * npo, r).T                                 # (n, nf*np)
+        return X0
+
+    def run_warm(self, freqs, n_train: int = 32, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
+                 chunk: int | None = None) -> SweepResult:
+        """Batched sweep: solve n_train evenly spread points, project every point onto
+        their span for its initial guess, then finish all points with batched GMRES."""
+        freqs = np.asarray(freqs, dtype=float)
+        nf, npo = len(freqs), len(self.ports)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tr = np.unique(np.round(np.linspace(0, nf - 1, min(n_train, nf))).astype(int))
+        first = self.run(freqs[tr], method="batched", tol=tol, restart=restart, max_iter=max_iter, chunk=chunk)
+        X0 = self.project(first.solutions, freqs)
+        rest = self.run(freqs, method="batched", tol=tol, restart=restart, max_iter=max_iter, x0=X0, chunk=chunk)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        info = {"train_points": len(tr), "train_iterations": first.iterations, "train_seconds": first.seconds,
+                "final_seconds": rest.seconds}
+        return SweepResult(freqs, rest.S, rest.iterations, rest.residuals, secs, rest.solutions, info)
+
+
+class _UnitRobin:
+    """A Robin BC with gamma = 1 and U_inc = E_mode (unit matrix / unit forcing)."""
+
+    def __init__(self, bc):
+        self.bc = bc
+        self.tags = bc.tags
+        self._include_stiff = bc._include_stiff
+        self._include_force = getattr(bc, "_include_force", False)
+        if hasattr(bc, "port_number"):
+            self.port_number = bc.port_number
+        if hasattr(bc, "cs"):
+            self.cs = bc.cs
+
+    def get_gamma(self, k0):
+        return 1.0 + 0j
+
+    def get_inv_basis(self):
+        return self.bc.get_inv_basis()
+
+    def get_Uinc(self, x, y, k0):
+        return np.asarray(self.bc.port_mode_3d(x, y, k0), dtype=np.complex128)
+
+
+def _mode_power(field, bc) -> float:
+    """int |E_mode|^2 over the port face with the 6-point rule (fem/mth/sparam.py:72-100)."""
+    from .freq import dunavant6
+    m = field.mesh
+    tri = np.asarray(m.get_triangles(bc.tags), dtype=np.int64)
+    tv = np.asarray(m.tris)[:, tri]
+    nodes = np.asarray(m.nodes)
+    D = dunavant6()
+    v1, v2, v3 = nodes[:, tv[0]], nodes[:, tv[1]], nodes[:, tv[2]]
+    area = np.linalg.norm(np.cross((v2 - v1).T, (v3 - v1).T), axis=1) / 2
+    tot = 0.0
+    for k in range(D.shape[1]):
+        p = v1 * D[1, k] + v2 * D[2, k] + v3 * D[3, k]
+        Em = bc.port_mode_3d_global(p[0], p[1], p[2], 1.0)
+        tot += D[0, k] * np.sum(np.sum(np.abs(Em) ** 2, axis=0) * area)
+    return float(tot)

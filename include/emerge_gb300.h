@@ -159,7 +159,7 @@ int emg_spmv(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_t Bm,
 int emg_rplan_gather(const emg_rplan* plan, int64_t Bc, const double* full, double* out, void* stream);
 int emg_rplan_scatter(const emg_rplan* plan, int64_t Bc, const double* x, double* full, void* stream);
 
-/* Right-preconditioned restarted GMRES(restart <= 64) with CGS2, columns in
+/* Right-preconditioned restarted GMRES(restart <= 256) with CGS2, columns in
  * lockstep; x holds the initial guess on entry.  Stops a column at relative
  * residual tol or after max_iter total iterations; iters_out (Bc int32) and
  * resid_out (Bc doubles, explicit ||b - A x|| / ||b||) are DEVICE arrays.

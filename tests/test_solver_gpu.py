@@ -1,0 +1,77 @@
+"""GPU solve path against the reference's SuperLU solutions and S-parameters (WR-90 guide).
+
+Tolerances: solutions within 1e-6 relative (GMRES stops at a 1e-10 relative
+residual), S-parameters within 1e-4 (linear units) of the reference.
+"""
+import numpy as np
+import pytest
+
+from _fixtures import load, waveguide_field_and_bcs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from emerge_gb300 import _build
+    _build.build()
+    return torch
+
+
+@pytest.fixture(scope="module")
+def waveguide(torch_cuda):
+    from emerge_gb300.freq import Assembler
+    z = load("waveguide.npz")
+    field, bcs = waveguide_field_and_bcs(z)
+    nT = field.mesh.n_tets
+    eye = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    return z, field, bcs, eye, Assembler()
+
+
+def test_gpu_solver_matches_superlu(waveguide):
+    """GPUSolver through the reference SolveRoutine contract: restricted system in, solution out."""
+    from emerge_gb300.solver import GPUSolver
+    z, field, bcs, eye, asm = waveguide
+    K, b, sid, pvs = asm.assemble_freq_matrix(field, eye, eye, bcs, float(z["freqs"][1]), cache_matrices=True)
+    A = K.tocsc()[sid][:, sid]
+    solver = GPUSolver(tol=1e-10)
+    for pn in (1, 2):
+        x_r, info = solver.solve(A, (b + pvs[pn])[sid], None, reuse_factorization=(pn == 2))
+        assert info == 0
+        x = np.zeros(K.shape[0], dtype=np.complex128)
+        x[sid] = x_r
+        ref = z[f"x1_{pn}"]
+        assert np.linalg.norm(x - ref) / np.linalg.norm(ref) <= 1e-6
+    assert solver.last_residual <= 1e-9
+
+
+@pytest.mark.parametrize("method", ["plain", "batched"])
+def test_sweep_sparams_match_reference(waveguide, method):
+    from emerge_gb300.solver import FrequencySweep
+    z, field, bcs, eye, asm = waveguide
+    sw = FrequencySweep(asm, field, eye, eye, bcs)
+    res = sw.run(z["freqs"], method=method, tol=1e-10)
+    assert np.all(res.residuals <= 1e-9)
+    assert np.max(np.abs(res.S - z["S"])) <= 1e-4
+    # solutions against SuperLU
+    X = sw.sys.scatter(res.solutions).cpu().numpy()          # (nf*np, N)
+    for f in range(len(z["freqs"])):
+        for p in range(2):
+            ref = z[f"x{f}_{p + 1}"]
+            assert np.linalg.norm(X[f * 2 + p] - ref) / np.linalg.norm(ref) <= 1e-6
+
+
+def test_warm_start_sweep_agrees_and_saves_iterations(waveguide):
+    """Reduced-basis warm start: same S-parameters as the plain sweep, fewer iterations."""
+    from emerge_gb300.solver import FrequencySweep
+    z, field, bcs, eye, asm = waveguide
+    sw = FrequencySweep(asm, field, eye, eye, bcs)
+    freqs = np.linspace(8.5e9, 10.5e9, 9)
+    cold = sw.run(freqs, method="batched", tol=1e-10)
+    warm = sw.run_warm(freqs, n_train=3, tol=1e-10)
+    assert np.all(warm.residuals <= 1e-9)
+    assert np.max(np.abs(warm.S - cold.S)) <= 1e-6
+    assert warm.iterations.sum() < cold.iterations.sum()
