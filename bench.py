@@ -257,6 +257,10 @@ def run_gpu(args, rank, world):
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
+    if rank == 0 and not args.no_sweep:
+        del E, B, pin_E, pin_B, npE, npB, plan
+        torch.cuda.empty_cache()
+        out["sweep"] = run_sweep(args)
     if rank == 0 and not args.no_cpu:
         nts, ti, tc = cpu_reference(field, er_s, args.cpu_sample)
         out["cpu_baseline"] = {"value": nts / (ti + tc), "unit": "tets/s", "cores": os.cpu_count(), "kind": "port",
@@ -264,6 +268,48 @@ def run_gpu(args, rank, world):
                                          f"reference element loop ({ti:.2f} s) + scipy coo.tocsr ({tc:.2f} s)"}
     if rank == 0:
         print(json.dumps(out))
+
+
+def run_sweep(args):
+    """Frequency sweep of the iris filter: batched + warm-started vs plain, both on the GPU.
+
+    freq-pts/s = points / wall time of the solve phase (matrices assembled before).
+    The plain method solves one frequency at a time (its own ILU(0), GMRES); it is
+    timed on ``--sweep-plain`` evenly spread points and its rate extrapolated.
+    max|dS| compares the warm-started sweep with the plain solves on those points.
+    """
+    import torch
+    from emerge_gb300.freq import Assembler
+    from emerge_gb300.geometry import iris_filter
+    from emerge_gb300.solver import FrequencySweep
+    p = iris_filter(args.sweep_h)
+    asm = Assembler()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sw = FrequencySweep(asm, p.field, p.er, p.ur, p.bcs)
+    torch.cuda.synchronize()
+    setup = time.perf_counter() - t0
+    nf = args.sweep_points
+    freqs = np.linspace(8e9, 12e9, nf)
+    idx = np.unique(np.linspace(0, nf - 1, args.sweep_plain).astype(int))
+    with ClockSampler(0) as clk:
+        warm = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), tol=args.sweep_tol)
+        plain = sw.run(freqs[idx], method="plain", tol=args.sweep_tol)
+    v_warm = nf / warm.seconds
+    v_plain = len(idx) / plain.seconds
+    dS = float(np.max(np.abs(warm.S[idx] - plain.S)))
+    return {
+        "workload": f"{p.name}: N={p.field.n_field} DOFs ({sw.sys.n} after PEC), {nf} points 8-12 GHz x 2 ports",
+        "metric": "sweep freq-pts/s", "batched_warm": v_warm, "plain": v_plain, "ratio": v_warm / v_plain,
+        "max_abs_dS_vs_plain": dS, "tol": args.sweep_tol, "setup_s": round(setup, 2),
+        "warm_seconds": round(warm.seconds, 2), "train_points": warm.info["train_points"],
+        "train_seconds": round(warm.info["train_seconds"], 2),
+        "iterations_warm_mean": float(warm.iterations.mean()), "iterations_warm_max": int(warm.iterations.max()),
+        "iterations_train_max": int(np.max(warm.info["train_iterations"])),
+        "iterations_plain_mean": float(plain.iterations.mean()), "plain_points_timed": int(len(idx)),
+        "ilu_levels": sw.sys.levels, "clocks": clk.summary(),
+        "S21_db_samples": [round(float(20 * np.log10(abs(v) + 1e-300)), 2) for v in warm.S[::max(1, nf // 8), 1, 0]],
+    }
 
 
 def main():
@@ -275,6 +321,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=200_000, help="tets in the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the frequency-sweep measurement")
+    ap.add_argument("--sweep-h", type=float, default=3e-3, help="iris-filter mesh size (m)")
+    ap.add_argument("--sweep-points", type=int, default=41)
+    ap.add_argument("--sweep-train", type=int, default=8)
+    ap.add_argument("--sweep-plain", type=int, default=2)
+    ap.add_argument("--sweep-tol", type=float, default=1e-8)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

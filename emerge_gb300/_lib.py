@@ -48,6 +48,22 @@ SIGNATURES = {
     "emg_rplan_scatter": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp]),
     "emg_gmres": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int,
                                  ctypes.c_double, c_vp, c_vp, c_vp]),
+    "emg_slab_create": (ctypes.c_int, [c_vp, c_vp, ctypes.POINTER(c_vp)]),
+    "emg_slab_destroy": (None, [c_vp]),
+    "emg_slab_info": (ctypes.c_int, [c_vp, c_vp]),
+    "emg_slab_levels": (ctypes.c_int, [c_vp, c_vp, c_vp]),
+    "emg_slab_factor": (ctypes.c_int, [c_vp, ctypes.c_int, c_i64, c_vp, c_i64, c_vp, c_vp]),
+    "emg_slab_apply": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "emg_gmres_slab": (ctypes.c_int, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_double, c_vp, c_vp, c_vp]),
+    "emg_mlp_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_uint64, ctypes.POINTER(c_vp)]),
+    "emg_mlp_nparam": (c_i64, [c_vp]),
+    "emg_mlp_get_params": (ctypes.c_int, [c_vp, c_vp]),
+    "emg_mlp_set_params": (ctypes.c_int, [c_vp, c_vp]),
+    "emg_mlp_forward": (ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp]),
+    "emg_mlp_train_step": (ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, ctypes.c_float, c_vp, c_vp, c_vp]),
+    "emg_mlp_destroy": (None, [c_vp]),
     "emg_csr_pattern_noalloc": (ctypes.c_int, [c_i64, c_i64, c_vp, c_vp, c_vp, c_i64, c_i64p, c_vp]),
 }
 

@@ -20,7 +20,7 @@
 #include <algorithm>
 #include <vector>
 
-#include "emg_common.cuh"
+#include "emg_krylov.cuh"
 
 namespace emg {
 namespace kry {
@@ -125,6 +125,68 @@ __global__ void k_trsv_level(int64_t nrows, const int32_t* __restrict__ rows, in
             for (int64_t k = rdiag[i] + 1; k < rptr[i + 1]; ++k) s = csub(s, cmul(LU[k * Bm + m], X[(int64_t)rind[k] * Bc + c]));
             X[i * Bc + c] = cdiv(s, LU[rdiag[i] * Bm + m]);
         }
+    }
+}
+
+// Small batches (Bc <= kSmallBc): warp per row, lanes over the row's nonzeros.
+constexpr int kSmallBc = 8;
+__global__ void k_trsv_level_w(int64_t nrows, const int32_t* __restrict__ rows, int64_t Bc,
+                               const int32_t* __restrict__ cmat, int64_t Bm, const int64_t* __restrict__ rptr,
+                               const int32_t* __restrict__ rind, const int64_t* __restrict__ rdiag,
+                               const double2* __restrict__ LU, int upper, double2* __restrict__ X) {
+    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wid >= nrows) return;
+    const int64_t i = rows[wid];
+    const int64_t k0 = upper ? rdiag[i] + 1 : rptr[i], k1 = upper ? rptr[i + 1] : rdiag[i];
+    double2 acc[kSmallBc];
+#pragma unroll
+    for (int c = 0; c < kSmallBc; ++c) acc[c] = make_double2(0.0, 0.0);
+    for (int64_t k = k0 + lane; k < k1; k += 32) {
+        const int64_t col = rind[k];
+#pragma unroll
+        for (int c = 0; c < kSmallBc; ++c)
+            if (c < Bc) acc[c] = cadd(acc[c], cmul(LU[k * Bm + cmat[c]], X[col * Bc + c]));
+    }
+#pragma unroll
+    for (int c = 0; c < kSmallBc; ++c) {
+        if (c >= Bc) break;
+        double2 v = acc[c];
+        for (int o = 16; o > 0; o >>= 1) {
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (lane == 0) {
+            const double2 s = csub(X[i * Bc + c], v);
+            X[i * Bc + c] = upper ? cdiv(s, LU[rdiag[i] * Bm + cmat[c]]) : s;
+        }
+    }
+}
+
+__global__ void k_spmv_w(int64_t n, int64_t Bc, const int32_t* __restrict__ cmat, int64_t Bm,
+                         const int64_t* __restrict__ rptr, const int32_t* __restrict__ rind, const double2* __restrict__ A,
+                         const double2* __restrict__ X, const double2* __restrict__ Bv, double2* __restrict__ Y) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    double2 acc[kSmallBc];
+#pragma unroll
+    for (int c = 0; c < kSmallBc; ++c) acc[c] = make_double2(0.0, 0.0);
+    for (int64_t k = rptr[i] + lane; k < rptr[i + 1]; k += 32) {
+        const int64_t col = rind[k];
+#pragma unroll
+        for (int c = 0; c < kSmallBc; ++c)
+            if (c < Bc) acc[c] = cadd(acc[c], cmul(A[k * Bm + cmat[c]], X[col * Bc + c]));
+    }
+#pragma unroll
+    for (int c = 0; c < kSmallBc; ++c) {
+        if (c >= Bc) break;
+        double2 v = acc[c];
+        for (int o = 16; o > 0; o >>= 1) {
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (lane == 0) Y[i * Bc + c] = Bv ? csub(Bv[i * Bc + c], v) : v;
     }
 }
 
@@ -340,28 +402,6 @@ __global__ void k_sqrt_real(int64_t Bc, const double2* __restrict__ in, double* 
 }  // namespace emg
 
 // ------------------------------------------------------------------ plan ---
-struct emg_rplan {
-    int64_t N = 0, ns = 0, nnz = 0, nnz_full = 0;
-    int64_t* sid = nullptr;       // solve ids (ns)
-    int32_t* map = nullptr;       // full -> restricted (N), -1 if removed
-    int64_t* rptr = nullptr;      // (ns+1)
-    int32_t* rind = nullptr;      // (nnz)
-    int64_t* rsrc = nullptr;      // (nnz) positions in the full pattern
-    int64_t* rdiag = nullptr;     // (ns)
-    int64_t* uptr = nullptr;      // (ns+1) factorization update lists
-    int64_t* ulist = nullptr;     // pairs (kk_local << 32 | pos in row k, target pos)
-    int32_t* lrows = nullptr;     // rows by forward level
-    int32_t* urows = nullptr;     // rows by backward level
-    std::vector<int64_t> lptr, uptr_lv;   // level boundaries (host)
-    // GMRES workspace (grown on demand)
-    size_t ws_bytes = 0;
-    void* ws = nullptr;
-    // private stream for graph capture of the Arnoldi step (the caller's stream may be
-    // the legacy default stream, which cannot be captured)
-    cudaStream_t gs = nullptr;
-    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-};
-
 namespace {
 using namespace emg;
 
@@ -530,15 +570,19 @@ extern "C" int emg_ilu0(const emg_rplan* p, int64_t Bm, double* LU, void* stream
 
 namespace {
 int trsv(const emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double2* LU, double2* X, cudaStream_t s) {
-    for (size_t l = 0; l + 1 < p->lptr.size(); ++l) {
-        const int64_t r0 = p->lptr[l], nr = p->lptr[l + 1] - r0;
-        kry::k_trsv_level<<<grid_for(nr * Bc, 128), 128, 0, s>>>(nr, p->lrows + r0, Bc, cmat, Bm, p->rptr, p->rind,
-                                                                 p->rdiag, LU, 0, X);
-    }
-    for (size_t l = 0; l + 1 < p->uptr_lv.size(); ++l) {
-        const int64_t r0 = p->uptr_lv[l], nr = p->uptr_lv[l + 1] - r0;
-        kry::k_trsv_level<<<grid_for(nr * Bc, 128), 128, 0, s>>>(nr, p->urows + r0, Bc, cmat, Bm, p->rptr, p->rind,
-                                                                 p->rdiag, LU, 1, X);
+    const bool small = Bc <= kry::kSmallBc;
+    for (int up = 0; up < 2; ++up) {
+        const std::vector<int64_t>& lv = up ? p->uptr_lv : p->lptr;
+        const int32_t* rows = up ? p->urows : p->lrows;
+        for (size_t l = 0; l + 1 < lv.size(); ++l) {
+            const int64_t r0 = lv[l], nr = lv[l + 1] - r0;
+            if (small)
+                kry::k_trsv_level_w<<<(unsigned)((nr * 32 + 127) / 128), 128, 0, s>>>(nr, rows + r0, Bc, cmat, Bm, p->rptr,
+                                                                                     p->rind, p->rdiag, LU, up, X);
+            else
+                kry::k_trsv_level<<<grid_for(nr * Bc, 128), 128, 0, s>>>(nr, rows + r0, Bc, cmat, Bm, p->rptr, p->rind,
+                                                                         p->rdiag, LU, up, X);
+        }
     }
     EMG_CUDA(cudaGetLastError());
     return EMG_OK;
@@ -594,6 +638,15 @@ extern "C" int emg_rplan_scatter(const emg_rplan* p, int64_t Bc, const double* x
 // implicit residual reaches tol * ||b||.  The final residual is recomputed
 // explicitly in FP64 (resid_out) after every restart.
 namespace {
+void spmv(const emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double2* A, const double2* X,
+          const double2* Bv, double2* Y, cudaStream_t s) {
+    const int64_t n = p->ns;
+    if (Bc <= kry::kSmallBc)
+        kry::k_spmv_w<<<(unsigned)((n * 32 + 127) / 128), 128, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, X, Bv, Y);
+    else
+        kry::k_spmv<<<grid_for(n * Bc, 256), 256, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, X, Bv, Y);
+}
+
 void dots(int64_t n, int64_t Bc, int nj, const double2* V, int64_t vstride, const double2* W, double2* part,
           int64_t nblk, cudaStream_t s) {
     if (Bc < 32) {
@@ -605,32 +658,27 @@ void dots(int64_t n, int64_t Bc, int nj, const double2* V, int64_t vstride, cons
 }
 }  // namespace
 
-extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A_,
-                         const double* LU_, const double* rhs_, double* x_, int restart, int max_iter, double tol,
-                         int32_t* iters_out, double* resid_out, void* stream) {
-    using namespace emg;
-    emg_rplan* p = const_cast<emg_rplan*>(pc);
-    EMG_CHECK_ARG(p && cmat && A_ && LU_ && rhs_ && x_ && iters_out && resid_out && Bc > 0 && Bm > 0,
-                  "emg_gmres: bad argument");
-    EMG_CHECK_ARG(restart >= 1 && restart <= kry::kMaxRestart && max_iter >= 1 && tol > 0,
-                  "emg_gmres: restart must be in [1, 256]");
-    cudaStream_t caller = (cudaStream_t)stream;
+namespace emg {
+int gmres_run(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double2* A, const double2* rhs,
+              double2* x, int restart, int max_iter, double tol, int32_t* iters_out, double* resid_out,
+              cudaStream_t caller, Precond& M, bool flexible) {
     const int64_t n = p->ns;
     if (n == 0) return EMG_OK;
+    {
+        const int rc = M.prepare(Bc);
+        if (rc) return rc;
+    }
     EMG_CUDA(cudaEventRecord(p->ev_in, caller));
     EMG_CUDA(cudaStreamWaitEvent(p->gs, p->ev_in, 0));
     cudaStream_t s = p->gs;
     const int m = restart;
-    const auto* A = reinterpret_cast<const double2*>(A_);
-    const auto* LU = reinterpret_cast<const double2*>(LU_);
-    const auto* rhs = reinterpret_cast<const double2*>(rhs_);
-    auto* x = reinterpret_cast<double2*>(x_);
     const int64_t vec = n * Bc;
     const int64_t nblk = (n + kry::kDotRows - 1) / kry::kDotRows;
     // workspace layout
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
     const size_t oV = take(sizeof(double2) * vec * (m + 1));
+    const size_t oZ = flexible ? take(sizeof(double2) * vec * m) : 0;
     const size_t oW = take(sizeof(double2) * vec);
     const size_t oT = take(sizeof(double2) * vec);
     const size_t oPart = take(sizeof(double2) * nblk * (m + 1) * Bc);
@@ -657,6 +705,7 @@ extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, i
     }
     char* base = static_cast<char*>(p->ws);
     auto* V = reinterpret_cast<double2*>(base + oV);
+    auto* Z = flexible ? reinterpret_cast<double2*>(base + oZ) : nullptr;
     auto* W = reinterpret_cast<double2*>(base + oW);
     auto* Tv = reinterpret_cast<double2*>(base + oT);
     auto* part = reinterpret_cast<double2*>(base + oPart);
@@ -687,10 +736,10 @@ extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, i
     // one Arnoldi step for Krylov index j (captured once per j into a CUDA graph)
     auto step = [&](int j) -> int {
         double2* Vj = V + (int64_t)j * vec;
-        EMG_CUDA(cudaMemcpyAsync(Tv, Vj, sizeof(double2) * vec, cudaMemcpyDeviceToDevice, s));
-        int rc = trsv(p, Bc, cmat, Bm, LU, Tv, s);
+        double2* Mv = flexible ? Z + (int64_t)j * vec : Tv;
+        int rc = M.apply(Vj, Mv, s);
         if (rc) return rc;
-        kry::k_spmv<<<grid_for(vec, T), T, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, Tv, nullptr, W);
+        spmv(p, Bc, cmat, Bm, A, Mv, nullptr, W, s);
         // CGS2: two passes of h = V^H w, w -= V h
         const unsigned hgrid = (unsigned)(((int64_t)(j + 1) * Bc + 127) / 128);
         dots(n, Bc, j + 1, V, vec, W, part, nblk, s);
@@ -716,7 +765,7 @@ extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, i
     std::vector<int32_t> hact(Bc), hprev(Bc), hits(Bc, 0);
     while (total < max_iter) {
         // r = b - A x ; V0 = r / ||r||
-        kry::k_spmv<<<grid_for(vec, T), T, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, x, rhs, W);
+        spmv(p, Bc, cmat, Bm, A, x, rhs, W, s);
         double2* rr = norms2(W);
         kry::k_restart_cols<<<cgrid, 128, 0, s>>>(Bc, rr, bn, tol, g, vs, act, len, res, m + 1);
         kry::k_scale_cols<<<grid_for(vec, T), T, 0, s>>>(n, Bc, vs, W, V);
@@ -752,19 +801,23 @@ extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, i
             }
             if (!any2) break;
         }
-        // x += M^-1 (V y)   (y from back substitution over each column's Krylov length)
+        // x += Z y (flexible) or x += M^-1 (V y)   (y from back substitution over each
+        // column's Krylov length)
         kry::k_backsolve<<<cgrid, 128, 0, s>>>(Bc, m, H, g, len, y, j);
-        EMG_CUDA(cudaMemsetAsync(Tv, 0, sizeof(double2) * vec, s));
-        kry::k_combine_basis<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j, V, vec, y, Tv);
-        {
-            int rc = trsv(p, Bc, cmat, Bm, LU, Tv, s);
+        if (flexible) {
+            EMG_CUDA(cudaMemsetAsync(Tv, 0, sizeof(double2) * vec, s));
+            kry::k_combine_basis<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j, Z, vec, y, Tv);
+        } else {
+            EMG_CUDA(cudaMemsetAsync(W, 0, sizeof(double2) * vec, s));
+            kry::k_combine_basis<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j, V, vec, y, W);
+            const int rc = M.apply(W, Tv, s);
             if (rc) return rc;
         }
         kry::k_axpy1<<<grid_for(vec, T), T, 0, s>>>(vec, Tv, x);
         EMG_CUDA(cudaGetLastError());
     }
     // explicit final residual
-    kry::k_spmv<<<grid_for(vec, T), T, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, x, rhs, W);
+    spmv(p, Bc, cmat, Bm, A, x, rhs, W, s);
     double2* rr = norms2(W);
     std::vector<double2> hr(Bc);
     std::vector<double> hb(Bc), hres(Bc);
@@ -778,4 +831,36 @@ extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, i
     EMG_CUDA(cudaEventRecord(p->ev_out, s));
     EMG_CUDA(cudaStreamWaitEvent(caller, p->ev_out, 0));
     return EMG_OK;
+}
+}  // namespace emg
+
+namespace {
+// ILU(0) factors as the preconditioner: out = (LU)^-1 in.
+struct IluPrecond : emg::Precond {
+    const emg_rplan* p;
+    int64_t Bc, Bm;
+    const int32_t* cmat;
+    const double2* LU;
+    IluPrecond(const emg_rplan* p_, int64_t Bc_, const int32_t* cmat_, int64_t Bm_, const double2* LU_)
+        : p(p_), Bc(Bc_), Bm(Bm_), cmat(cmat_), LU(LU_) {}
+    int apply(const double2* in, double2* out, cudaStream_t s) override {
+        EMG_CUDA(cudaMemcpyAsync(out, in, sizeof(double2) * p->ns * Bc, cudaMemcpyDeviceToDevice, s));
+        return trsv(p, Bc, cmat, Bm, LU, out, s);
+    }
+};
+}  // namespace
+
+extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A_,
+                         const double* LU_, const double* rhs_, double* x_, int restart, int max_iter, double tol,
+                         int32_t* iters_out, double* resid_out, void* stream) {
+    using namespace emg;
+    emg_rplan* p = const_cast<emg_rplan*>(pc);
+    EMG_CHECK_ARG(p && cmat && A_ && LU_ && rhs_ && x_ && iters_out && resid_out && Bc > 0 && Bm > 0,
+                  "emg_gmres: bad argument");
+    EMG_CHECK_ARG(restart >= 1 && restart <= kry::kMaxRestart && max_iter >= 1 && tol > 0,
+                  "emg_gmres: restart must be in [1, 256]");
+    IluPrecond M(p, Bc, cmat, Bm, reinterpret_cast<const double2*>(LU_));
+    return gmres_run(p, Bc, cmat, Bm, reinterpret_cast<const double2*>(A_), reinterpret_cast<const double2*>(rhs_),
+                     reinterpret_cast<double2*>(x_), restart, max_iter, tol, iters_out, resid_out, (cudaStream_t)stream,
+                     M, false);
 }

@@ -1,0 +1,50 @@
+// Restricted system plan and the preconditioner-generic GMRES driver shared by
+// the ILU(0) path (emg_krylov.cu) and the slab factorization (emg_slab.cu).
+#pragma once
+
+#include <vector>
+
+#include "emg_common.cuh"
+
+struct emg_rplan {
+    int64_t N = 0, ns = 0, nnz = 0, nnz_full = 0;
+    int64_t* sid = nullptr;       // solve ids (ns)
+    int32_t* map = nullptr;       // full -> restricted (N), -1 if removed
+    int64_t* rptr = nullptr;      // (ns+1)
+    int32_t* rind = nullptr;      // (nnz)
+    int64_t* rsrc = nullptr;      // (nnz) positions in the full pattern
+    int64_t* rdiag = nullptr;     // (ns)
+    int64_t* uptr = nullptr;      // (ns+1) factorization update lists
+    int64_t* ulist = nullptr;     // pairs (kk_local << 32 | pos in row k, target pos)
+    int32_t* lrows = nullptr;     // rows by forward level
+    int32_t* urows = nullptr;     // rows by backward level
+    std::vector<int64_t> lptr, uptr_lv;   // level boundaries (host)
+    // GMRES workspace (grown on demand)
+    size_t ws_bytes = 0;
+    void* ws = nullptr;
+    // private stream for graph capture of the Arnoldi step (the caller's stream may be
+    // the legacy default stream, which cannot be captured)
+    cudaStream_t gs = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+};
+
+namespace emg {
+
+// Right preconditioner M^-1 applied to Bc columns (vectors [n][Bc], complex
+// double).  prepare() runs before any stream capture and does every allocation;
+// apply() is captured into CUDA graphs, so it may only enqueue work on ``s``.
+struct Precond {
+    virtual ~Precond() = default;
+    virtual int prepare(int64_t Bc) { (void)Bc; return EMG_OK; }
+    virtual int apply(const double2* in, double2* out, cudaStream_t s) = 0;   // in and out do not alias
+};
+
+// Restarted GMRES(restart) with CGS2 over Bc lockstep columns (column c uses
+// matrix cmat[c] of Bm).  flexible: keep z_j = M^-1 v_j and update x with them
+// (FGMRES, required when M^-1 is not an exact fixed linear map, e.g. a
+// reduced-precision factorization); otherwise x += M^-1 (V y).
+int gmres_run(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double2* A, const double2* rhs,
+              double2* x, int restart, int max_iter, double tol, int32_t* iters_out, double* resid_out,
+              cudaStream_t caller, Precond& M, bool flexible);
+
+}  // namespace emg

@@ -1,0 +1,872 @@
+// Slab factorization: a direct block-tridiagonal solver for the restricted
+// frequency-domain system, used as the preconditioner of a flexible GMRES.
+//
+// Replaces the direct sparse solve of SolveRoutine (SuperLU / PARDISO / UMFPACK,
+// fem/solver.py:220-309, 405-469) for guided-wave structures.  The level-scheduled
+// ILU(0) of emg_krylov.cu does not converge on resonant structures (iris filters),
+// so a sweep needs a factorization that is exact up to rounding.
+//
+// Structure.  A breadth-first search from a pseudo-peripheral DOF splits the
+// restricted DOFs into level sets ("slabs"); every matrix entry couples DOFs of the
+// same slab or of neighbouring slabs, so A is block tridiagonal:
+//     A = tridiag(C_i, D_i, U_i),  C_i = A[L_i, L_{i-1}],  U_i = A[L_i, L_{i+1}].
+// On a waveguide the slabs are cross-sections and their widths stay near the DOF
+// count of one cross-section.  Block elimination gives
+//     S_0 = D_0,  S_i = D_i - C_i S_{i-1}^-1 U_{i-1}
+// and the factor stores the dense inverses S_i^-1 (complex FP32 or FP64), plus
+// the sparse couplings C_i, U_i.  A solve is then, per slab, a sparse product and
+// one dense matrix x block-of-vectors product forward, the same backward:
+//     z_i = S_i^-1 (b_i - C_i z_{i-1}),   x_i = z_i - S_i^-1 U_i x_{i+1}.
+//
+// Kernels.  S_i - C_i S_{i-1}^-1 U_{i-1} is one launch per slab: a CTA owns a few
+// rows, builds R = C S^-1 for them in shared memory from coalesced rows of S^-1,
+// then multiplies by the sparse U columns.  S_i^-1 is computed in place by blocked
+// Gauss-Jordan with 64 x 64 tiles: the pivot tile is inverted by one CTA with
+// partial pivoting inside the tile (a pivot below a relative threshold is replaced
+// by the threshold and counted), the pivot row panel is multiplied by it, every
+// other tile gets a rank-64 update (the bulk of the flops, a tiled complex GEMM),
+// and the pivot column panel is multiplied by minus it.  Several factorizations
+// (anchor frequencies) run in the same launches (grid z), each with its own values.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "emg_krylov.cuh"
+
+namespace emg {
+namespace slab {
+
+template <typename R> struct C2;
+template <> struct C2<float> { using T = float2; };
+template <> struct C2<double> { using T = double2; };
+
+__device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
+template <typename T> __device__ __forceinline__ T czero() { T z; z.x = 0; z.y = 0; return z; }
+template <typename T> __device__ __forceinline__ void cfma(T& acc, T a, T b) {   // acc += a b
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+template <typename T> __device__ __forceinline__ T cmul(T a, T b) { return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+template <typename T> __device__ __forceinline__ T cvt(double2 v);
+template <> __device__ __forceinline__ float2 cvt<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
+template <> __device__ __forceinline__ double2 cvt<double2>(double2 v) { return v; }
+__device__ __forceinline__ double2 to_d(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 to_d(double2 v) { return v; }
+
+constexpr int kTile = 64;          // Gauss-Jordan tile and GEMM output tile
+constexpr int kThreads = 256;
+constexpr int kMaxRows = 16;       // rows per CTA in the Schur-complement kernel
+constexpr int kSchurSmem = 200 * 1024;
+constexpr int64_t kMaxWidth = 12288;
+
+template <typename R> struct Tile {
+    using T = typename C2<R>::T;
+    static constexpr int BK = sizeof(R) == 4 ? 16 : 8;
+    static constexpr int LA = kTile * BK / kThreads;   // A elements per thread and chunk
+    T a[2][BK][kTile + 1];
+    T b[2][BK][kTile];
+};
+
+// acc[i][j] (row ty+16i, column tx+16j of the 64 x 64 output tile) += A B with
+// A (M x K, row-major lda) and B (K x N, row-major ldb), M, N <= 64.  Zero fill
+// outside.  Double-buffered through shared memory, one barrier per K chunk.
+template <typename R>
+__device__ __forceinline__ void tile_mac(typename C2<R>::T (&acc)[4][4], const typename C2<R>::T* __restrict__ A,
+                                         int64_t lda, const typename C2<R>::T* __restrict__ B, int64_t ldb, int M,
+                                         int N, int64_t K, Tile<R>& sm) {
+    using T = typename C2<R>::T;
+    constexpr int BK = Tile<R>::BK, LA = Tile<R>::LA;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    T ra[LA], rb[LA];
+    auto load = [&](int64_t k0) {
+#pragma unroll
+        for (int q = 0; q < LA; ++q) {
+            const int idx = tid + kThreads * q;
+            const int r = idx / BK, kk = idx % BK;
+            ra[q] = (r < M && k0 + kk < K) ? A[(int64_t)r * lda + k0 + kk] : czero<T>();
+            const int kb = idx / kTile, c = idx % kTile;
+            rb[q] = (c < N && k0 + kb < K) ? B[(k0 + kb) * ldb + c] : czero<T>();
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int q = 0; q < LA; ++q) {
+            const int idx = tid + kThreads * q;
+            sm.a[buf][idx % BK][idx / BK] = ra[q];
+            sm.b[buf][idx / kTile][idx % kTile] = rb[q];
+        }
+    };
+    load(0);
+    store(0);
+    __syncthreads();
+    int buf = 0;
+    for (int64_t k0 = 0; k0 < K; k0 += BK) {
+        const bool more = k0 + BK < K;
+        if (more) load(k0 + BK);
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            T av[4], bv[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) av[i] = sm.a[buf][kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bv[j] = sm.b[buf][kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) cfma(acc[i][j], av[i], bv[j]);
+        }
+        if (more) store(buf ^ 1);
+        __syncthreads();
+        buf ^= 1;
+    }
+}
+
+// ------------------------------------------------------------ factorization ---
+// Dense blocks D_i and the sparse couplings of F matrices: column amat[f] of A
+// ([nnz][Bm]) goes to factor f.
+template <typename R>
+__global__ void k_values(int64_t nnz, int64_t Bm, int64_t F, const int32_t* __restrict__ amat,
+                         const double2* __restrict__ A, const int64_t* __restrict__ dmap, int64_t totD,
+                         typename C2<R>::T* __restrict__ D) {
+    using T = typename C2<R>::T;
+    const int64_t total = nnz * F;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t / F, f = t % F;
+        const int64_t d = dmap[e];
+        if (d >= 0) D[f * totD + d] = cvt<T>(A[e * Bm + amat[f]]);
+    }
+}
+
+template <typename R>
+__global__ void k_offvals(int64_t nn, int64_t Bm, int64_t F, const int32_t* __restrict__ amat,
+                          const double2* __restrict__ A, const int64_t* __restrict__ src,
+                          typename C2<R>::T* __restrict__ out) {
+    using T = typename C2<R>::T;
+    const int64_t total = nn * F;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = t % nn, f = t / nn;
+        out[t] = cvt<T>(A[src[k] * Bm + amat[f]]);
+    }
+}
+
+// S_i -= (C_i S_{i-1}^-1) U_{i-1} for rows [a0, a0+nr) of slab i (grid: row blocks x 1 x F).
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_schur(int64_t wp, int64_t w, int64_t row0, int rb,
+                                                    const int64_t* __restrict__ cptr, const int32_t* __restrict__ cidx,
+                                                    const typename C2<R>::T* __restrict__ Cval, int64_t nC,
+                                                    const int64_t* __restrict__ ucptr, const int32_t* __restrict__ ucrow,
+                                                    const typename C2<R>::T* __restrict__ UCval, int64_t nU,
+                                                    typename C2<R>::T* __restrict__ Sinv, int64_t totD, int64_t offPrev,
+                                                    int64_t offCur) {
+    using T = typename C2<R>::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* Rs = reinterpret_cast<T*>(smem_raw);
+    const int64_t f = blockIdx.z;
+    const int64_t a0 = (int64_t)blockIdx.x * rb;
+    const int nr = (int)min((int64_t)rb, w - a0);
+    const T* Sp = Sinv + f * totD + offPrev;
+    T* Sc = Sinv + f * totD + offCur;
+    const T* Cv = Cval + f * nC;
+    const T* Uv = UCval + f * nU;
+    for (int64_t idx = threadIdx.x; idx < (int64_t)nr * wp; idx += blockDim.x) {
+        const int64_t a = idx / wp, col = idx % wp;
+        const int64_t row = row0 + a0 + a;
+        T acc = czero<T>();
+        for (int64_t k = cptr[row]; k < cptr[row + 1]; ++k) cfma(acc, Cv[k], Sp[(int64_t)cidx[k] * wp + col]);
+        Rs[idx] = acc;
+    }
+    __syncthreads();
+    for (int64_t j = threadIdx.x; j < w; j += blockDim.x) {
+        T acc[kMaxRows];
+#pragma unroll
+        for (int a = 0; a < kMaxRows; ++a) acc[a] = czero<T>();
+        for (int64_t k = ucptr[row0 + j]; k < ucptr[row0 + j + 1]; ++k) {
+            const int64_t r = ucrow[k];
+            const T u = Uv[k];
+#pragma unroll
+            for (int a = 0; a < kMaxRows; ++a)
+                if (a < nr) cfma(acc[a], Rs[a * wp + r], u);
+        }
+#pragma unroll
+        for (int a = 0; a < kMaxRows; ++a)
+            if (a < nr) {
+                T& s = Sc[(a0 + a) * w + j];
+                s.x -= acc[a].x;
+                s.y -= acc[a].y;
+            }
+    }
+}
+
+// In-place inverse of pivot tile k (tb x tb) with partial pivoting inside the tile;
+// the inverse also goes to pinv (ld 64).  Grid 1 x 1 x F.
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
+                                                      int64_t totD, int64_t offD, typename C2<R>::T* __restrict__ pinv,
+                                                      R rel_thr, int32_t* __restrict__ perturbed) {
+    using T = typename C2<R>::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T(*a)[kTile + 1] = reinterpret_cast<T(*)[kTile + 1]>(smem_raw);
+    __shared__ int piv[kTile];
+    __shared__ int s_p;
+    __shared__ R s_red[kThreads / 32];
+    const int64_t f = blockIdx.z;
+    T* M = Sinv + f * totD + offD;
+    const int64_t k0 = (int64_t)k * kTile;
+    const int tb = (int)min((int64_t)kTile, w - k0);
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    R mx = 0;
+    for (int idx = tid; idx < tb * tb; idx += kThreads) {
+        const int r = idx / tb, c = idx % tb;
+        const T v = M[(k0 + r) * w + k0 + c];
+        a[r][c] = v;
+        mx = max(mx, v.x * v.x + v.y * v.y);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s_red[wid] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        R m2 = 0;
+        for (int i = 0; i < kThreads / 32; ++i) m2 = max(m2, s_red[i]);
+        s_red[0] = m2;
+    }
+    __syncthreads();
+    const R thr2 = s_red[0] * rel_thr * rel_thr;   // |pivot|^2 below this is replaced
+    constexpr int kPer = kTile * kTile / kThreads;
+    T vals[kPer];
+    for (int c = 0; c < tb; ++c) {
+        if (wid == 0) {
+            R best = -1;
+            int bi = c;
+            for (int r = c + lane; r < tb; r += 32) {
+                const R m2 = a[r][c].x * a[r][c].x + a[r][c].y * a[r][c].y;
+                if (m2 > best) { best = m2; bi = r; }
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                const R ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) { s_p = bi; piv[c] = bi; }
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p != c && tid < tb) {
+            const T t = a[p][tid];
+            a[p][tid] = a[c][tid];
+            a[c][tid] = t;
+        }
+        __syncthreads();
+        T pv = a[c][c];
+        R m2 = pv.x * pv.x + pv.y * pv.y;
+        if (!(m2 > thr2)) {   // also catches a zero pivot of an all-zero tile
+            pv = mk(sqrt(thr2) > 0 ? (R)sqrt(thr2) : (R)1, (R)0);
+            m2 = pv.x * pv.x;
+            if (tid == 0) atomicAdd(perturbed + f, 1);
+        }
+        const T inv = mk(pv.x / m2, -pv.y / m2);
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int idx = tid + kThreads * q;
+            const int r = idx / kTile, j = idx % kTile;
+            if (r >= tb || j >= tb) continue;
+            T v;
+            if (r == c && j == c) v = inv;
+            else if (r == c) v = cmul(a[c][j], inv);
+            else if (j == c) { const T t = cmul(a[r][c], inv); v = mk(-t.x, -t.y); }
+            else { v = a[r][j]; const T t = cmul(a[r][c], inv); const T u = cmul(t, a[c][j]); v.x -= u.x; v.y -= u.y; }
+            vals[q] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int idx = tid + kThreads * q;
+            const int r = idx / kTile, j = idx % kTile;
+            if (r < tb && j < tb) a[r][j] = vals[q];
+        }
+        __syncthreads();
+    }
+    // undo the row interchanges as column interchanges, last first
+    for (int c = tb - 1; c >= 0; --c) {
+        const int p = piv[c];
+        if (p != c && tid < tb) {
+            const T t = a[tid][p];
+            a[tid][p] = a[tid][c];
+            a[tid][c] = t;
+        }
+        __syncthreads();
+    }
+    T* P = pinv + f * kTile * kTile;
+    for (int idx = tid; idx < tb * tb; idx += kThreads) {
+        const int r = idx / tb, c = idx % tb;
+        M[(k0 + r) * w + k0 + c] = a[r][c];
+        P[r * kTile + c] = a[r][c];
+    }
+}
+
+// mode 0: row panel  M[k, c] = Pinv M[k, c]       (grid: column tiles x 1 x F, c != k)
+// mode 1: col panel  M[r, k] = -M[r, k] Pinv      (grid: row tiles x 1 x F, r != k)
+// mode 2: update     M[r, c] -= M[r, k] M[k, c]   (grid: column tiles x row tiles x F, r, c != k)
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_gj_panel(int mode, int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
+                                                       int64_t totD, int64_t offD, const typename C2<R>::T* __restrict__ pinv) {
+    using T = typename C2<R>::T;
+    __shared__ Tile<R> sm;
+    const int64_t f = blockIdx.z;
+    T* M = Sinv + f * totD + offD;
+    const T* P = pinv + f * kTile * kTile;
+    const int64_t k0 = (int64_t)k * kTile;
+    const int tb = (int)min((int64_t)kTile, w - k0);
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
+    int64_t r0, c0;
+    int nr, nc;
+    T* out;
+    if (mode == 0) {
+        if ((int)blockIdx.x == k) return;
+        c0 = (int64_t)blockIdx.x * kTile;
+        nc = (int)min((int64_t)kTile, w - c0);
+        nr = tb;
+        out = M + k0 * w + c0;
+        tile_mac<R>(acc, P, kTile, out, w, nr, nc, tb, sm);
+    } else if (mode == 1) {
+        if ((int)blockIdx.x == k) return;
+        r0 = (int64_t)blockIdx.x * kTile;
+        nr = (int)min((int64_t)kTile, w - r0);
+        nc = tb;
+        out = M + r0 * w + k0;
+        tile_mac<R>(acc, out, w, P, kTile, nr, nc, tb, sm);
+    } else {
+        if ((int)blockIdx.x == k || (int)blockIdx.y == k) return;
+        r0 = (int64_t)blockIdx.y * kTile;
+        c0 = (int64_t)blockIdx.x * kTile;
+        nr = (int)min((int64_t)kTile, w - r0);
+        nc = (int)min((int64_t)kTile, w - c0);
+        out = M + r0 * w + c0;
+        tile_mac<R>(acc, M + r0 * w + k0, w, M + k0 * w + c0, w, nr, nc, tb, sm);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = ty + 16 * i, c = tx + 16 * j;
+            if (r < nr && c < nc) {
+                T& o = out[(int64_t)r * w + c];
+                if (mode == 0) o = acc[i][j];
+                else if (mode == 1) o = mk(-acc[i][j].x, -acc[i][j].y);
+                else { o.x -= acc[i][j].x; o.y -= acc[i][j].y; }
+            }
+        }
+}
+
+// ------------------------------------------------------------------- solve ---
+template <typename R>
+__global__ void k_gather(int64_t n, int64_t Bc, const int32_t* __restrict__ perm, const double2* __restrict__ X,
+                         typename C2<R>::T* __restrict__ Y) {
+    using T = typename C2<R>::T;
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = t / Bc, c = t % Bc;
+        Y[t] = cvt<T>(X[(int64_t)perm[pos] * Bc + c]);
+    }
+}
+
+template <typename R>
+__global__ void k_scatter(int64_t n, int64_t Bc, const int32_t* __restrict__ perm, const typename C2<R>::T* __restrict__ Z,
+                          double2* __restrict__ X) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = t / Bc, c = t % Bc;
+        X[(int64_t)perm[pos] * Bc + c] = to_d(Z[t]);
+    }
+}
+
+// mode 0: Y[row] -= sum C[row,k] Z[prev0 + cidx[k]]    (forward coupling)
+// mode 1: Y[row]  = sum U[row,k] Z[next0 + uidx[k]]    (backward coupling)
+template <typename R>
+__global__ void k_couple(int mode, int64_t w, int64_t row0, int64_t nb0, int64_t Bc, const int32_t* __restrict__ colfac,
+                         const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                         const typename C2<R>::T* __restrict__ val, int64_t nval, const typename C2<R>::T* __restrict__ Z,
+                         typename C2<R>::T* __restrict__ Y) {
+    using T = typename C2<R>::T;
+    const int64_t total = w * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = row0 + t / Bc, c = t % Bc;
+        const T* v = val + (int64_t)colfac[c] * nval;
+        T s = czero<T>();
+        for (int64_t k = ptr[row]; k < ptr[row + 1]; ++k) cfma(s, v[k], Z[(nb0 + idx[k]) * Bc + c]);
+        T& y = Y[row * Bc + c];
+        if (mode == 0) { y.x -= s.x; y.y -= s.y; }
+        else y = s;
+    }
+}
+
+struct Group {
+    int32_t fac, col0, ncol, pad;
+};
+
+// Out[r, cols of group g] = beta Out + alpha S_i^-1[r, :] Y[:, cols]: warp per row,
+// lanes over the row of S_i^-1 (coalesced), 16 columns per pass.  Grid: row blocks x groups.
+constexpr int kRowCols = 16;
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_rowmv(int64_t w, int64_t row0, int64_t Bc, const Group* __restrict__ groups,
+                                                    const typename C2<R>::T* __restrict__ Sinv, int64_t totD, int64_t offD,
+                                                    const typename C2<R>::T* __restrict__ Y, R alpha, int beta,
+                                                    typename C2<R>::T* __restrict__ Out) {
+    using T = typename C2<R>::T;
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= w) return;
+    const Group g = groups[blockIdx.y];
+    const T* S = Sinv + (int64_t)g.fac * totD + offD + r * w;
+    const T* Yb = Y + row0 * Bc;
+    for (int c0 = 0; c0 < g.ncol; c0 += kRowCols) {
+        const int nc = min(kRowCols, g.ncol - c0);
+        const int64_t cb = g.col0 + c0;
+        T acc[kRowCols];
+#pragma unroll
+        for (int j = 0; j < kRowCols; ++j) acc[j] = czero<T>();
+        for (int64_t k = lane; k < w; k += 32) {
+            const T s = S[k];
+            const T* yr = Yb + k * Bc + cb;
+#pragma unroll
+            for (int j = 0; j < kRowCols; ++j)
+                if (j < nc) cfma(acc[j], s, yr[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < kRowCols; ++j) {
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                acc[j].x += __shfl_xor_sync(0xffffffffu, acc[j].x, o);
+                acc[j].y += __shfl_xor_sync(0xffffffffu, acc[j].y, o);
+            }
+        }
+        if (lane < nc) {
+            T v = acc[0];
+#pragma unroll
+            for (int j = 1; j < kRowCols; ++j)
+                if (j == lane) v = acc[j];
+            T& o = Out[(row0 + r) * Bc + cb + lane];
+            const T res = mk(alpha * v.x, alpha * v.y);
+            if (beta) { o.x += res.x; o.y += res.y; }
+            else o = res;
+        }
+    }
+}
+
+}  // namespace slab
+}  // namespace emg
+
+// ------------------------------------------------------------------- plan ---
+struct emg_slab {
+    emg_rplan* rp = nullptr;
+    int64_t n = 0, nnz = 0;
+    int m = 0;
+    std::vector<int64_t> off, offD;   // slab boundaries (positions), dense block offsets
+    int64_t totD = 0, maxw = 0, nC = 0, nU = 0;
+    int32_t* perm = nullptr;          // slab position -> restricted index
+    int64_t* dmap = nullptr;          // restricted entry -> dense index or -1
+    int64_t *cptr = nullptr, *csrc = nullptr;
+    int32_t* cidx = nullptr;
+    int64_t *uptr = nullptr, *usrc = nullptr;
+    int32_t* uidx = nullptr;
+    int64_t *ucptr = nullptr, *ucsrc = nullptr;
+    int32_t* ucrow = nullptr;
+    // factors
+    int prec = 0;                     // 1 complex FP32, 2 complex FP64
+    int64_t F = 0;
+    void *Sinv = nullptr, *Cval = nullptr, *Uval = nullptr, *UCval = nullptr, *pinv = nullptr;
+    int32_t* perturbed = nullptr;
+    int64_t n_perturbed = 0;
+    // solve workspace
+    int64_t ws_cols = 0;
+    void *Y = nullptr, *Z = nullptr;
+    int32_t* colfac = nullptr;
+    emg::slab::Group* groups = nullptr;
+    int64_t ngroups_cap = 0;
+};
+
+namespace {
+using namespace emg;
+
+void slab_free_factors(emg_slab* s) {
+    dfree(s->Sinv); dfree(s->Cval); dfree(s->Uval); dfree(s->UCval); dfree(s->pinv); dfree(s->perturbed);
+    s->F = 0;
+    s->prec = 0;
+}
+
+void slab_free(emg_slab* s) {
+    if (!s) return;
+    slab_free_factors(s);
+    dfree(s->perm); dfree(s->dmap); dfree(s->cptr); dfree(s->csrc); dfree(s->cidx); dfree(s->uptr); dfree(s->usrc);
+    dfree(s->uidx); dfree(s->ucptr); dfree(s->ucsrc); dfree(s->ucrow); dfree(s->Y); dfree(s->Z); dfree(s->colfac);
+    dfree(s->groups);
+    delete s;
+}
+
+template <typename V>
+int upload(V** d, const std::vector<V>& h, const char* what) {
+    int rc = dalloc(d, (int64_t)std::max<size_t>(h.size(), 1), what);
+    if (rc) return rc;
+    if (!h.empty()) EMG_CUDA(cudaMemcpy(*d, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice));
+    return EMG_OK;
+}
+
+// Breadth-first levels over the nodes not yet placed; returns the nodes of the
+// component of ``start`` in level order (lev filled, levels numbered from base).
+std::vector<int64_t> bfs(int64_t start, const std::vector<int64_t>& ptr, const std::vector<int32_t>& ind,
+                         std::vector<int32_t>& lev, int32_t base) {
+    std::vector<int64_t> order{start};
+    lev[start] = base;
+    for (size_t h = 0; h < order.size(); ++h) {
+        const int64_t v = order[h];
+        for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
+            const int64_t u = ind[k];
+            if (lev[u] < 0) {
+                lev[u] = lev[v] + 1;
+                order.push_back(u);
+            }
+        }
+    }
+    return order;
+}
+}  // namespace
+
+extern "C" int emg_slab_create(const emg_rplan* rp, void* stream, emg_slab** out) {
+    using namespace emg;
+    EMG_CHECK_ARG(rp && out, "emg_slab_create: NULL argument");
+    *out = nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n = rp->ns, nnz = rp->nnz;
+    std::vector<int64_t> ptr(n + 1);
+    std::vector<int32_t> ind(nnz);
+    EMG_CUDA(cudaMemcpyAsync(ptr.data(), rp->rptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st));
+    if (nnz) EMG_CUDA(cudaMemcpyAsync(ind.data(), rp->rind, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, st));
+    EMG_CUDA(cudaStreamSynchronize(st));
+    // levels: per connected component, BFS from a pseudo-peripheral node (three
+    // sweeps, each restarting from a minimum-degree node of the last level)
+    std::vector<int32_t> lev(n, -1), tmp(n, -1);
+    int32_t base = 0;
+    for (int64_t s0 = 0; s0 < n; ++s0) {
+        if (lev[s0] >= 0) continue;
+        int64_t start = s0;
+        for (int sweep = 0; sweep < 3; ++sweep) {
+            std::vector<int64_t> ord = bfs(start, ptr, ind, tmp, 0);
+            const int32_t last = tmp[ord.back()];
+            int64_t best = ord.back();
+            for (auto it = ord.rbegin(); it != ord.rend() && tmp[*it] == last; ++it)
+                if (ptr[*it + 1] - ptr[*it] < ptr[best + 1] - ptr[best] ||
+                    (ptr[*it + 1] - ptr[*it] == ptr[best + 1] - ptr[best] && *it < best))
+                    best = *it;
+            for (int64_t v : ord) tmp[v] = -1;
+            start = best;
+        }
+        std::vector<int64_t> ord = bfs(start, ptr, ind, lev, base);
+        int32_t top = base;
+        for (int64_t v : ord) top = std::max(top, lev[v]);
+        base = top + 1;
+    }
+    const int m = base;
+    auto* s = new emg_slab();
+    s->rp = const_cast<emg_rplan*>(rp);
+    s->n = n;
+    s->nnz = nnz;
+    s->m = m;
+    s->off.assign(m + 1, 0);
+    for (int64_t v = 0; v < n; ++v) s->off[lev[v] + 1]++;
+    for (int i = 0; i < m; ++i) s->off[i + 1] += s->off[i];
+    s->offD.assign(m + 1, 0);
+    for (int i = 0; i < m; ++i) {
+        const int64_t w = s->off[i + 1] - s->off[i];
+        s->maxw = std::max(s->maxw, w);
+        s->offD[i + 1] = s->offD[i] + w * w;
+    }
+    s->totD = s->offD[m];
+    if (s->maxw > slab::kMaxWidth) {
+        delete s;
+        set_error("emg_slab_create: a slab is wider than 12288 DOFs (structure not slab-like)");
+        return EMG_ERR_LIMIT;
+    }
+    // positions: slabs in order, restricted index ascending inside a slab
+    std::vector<int32_t> perm(n);
+    std::vector<int64_t> ipos(n), fill(s->off.begin(), s->off.end() - 1);
+    for (int64_t v = 0; v < n; ++v) {
+        const int64_t p = fill[lev[v]]++;
+        perm[p] = (int32_t)v;
+        ipos[v] = p;
+    }
+    std::vector<int64_t> dmap(nnz, -1), cptr(n + 1, 0), uptr(n + 1, 0), ucptr(n + 1, 0);
+    // count
+    for (int64_t r = 0; r < n; ++r) {
+        const int32_t lr = lev[r];
+        for (int64_t k = ptr[r]; k < ptr[r + 1]; ++k) {
+            const int64_t c = ind[k];
+            const int32_t lc = lev[c];
+            if (lc == lr - 1) cptr[ipos[r] + 1]++;
+            else if (lc == lr + 1) { uptr[ipos[r] + 1]++; ucptr[ipos[c] + 1]++; }
+            else if (lc != lr) {
+                delete s;
+                set_error("emg_slab_create: entry couples non-adjacent slabs");
+                return EMG_ERR_MESH;
+            }
+        }
+    }
+    for (int64_t i = 0; i < n; ++i) { cptr[i + 1] += cptr[i]; uptr[i + 1] += uptr[i]; ucptr[i + 1] += ucptr[i]; }
+    s->nC = cptr[n];
+    s->nU = uptr[n];
+    std::vector<int32_t> cidx(s->nC), uidx(s->nU), ucrow(s->nU);
+    std::vector<int64_t> csrc(s->nC), usrc(s->nU), ucsrc(s->nU);
+    std::vector<int64_t> cf(cptr.begin(), cptr.end() - 1), uf(uptr.begin(), uptr.end() - 1), ucf(ucptr.begin(), ucptr.end() - 1);
+    // rows in slab-position order so each row's entries come out sorted by column position
+    for (int64_t p = 0; p < n; ++p) {
+        const int64_t r = perm[p];
+        const int32_t lr = lev[r];
+        std::vector<std::pair<int64_t, int64_t>> ents;   // (column position, entry)
+        for (int64_t k = ptr[r]; k < ptr[r + 1]; ++k) ents.emplace_back(ipos[ind[k]], k);
+        std::sort(ents.begin(), ents.end());
+        for (auto& pe : ents) {
+            const int64_t pc = pe.first, k = pe.second;
+            const int32_t lc = lev[perm[pc]];
+            if (lc == lr) {
+                const int64_t w = s->off[lr + 1] - s->off[lr];
+                dmap[k] = s->offD[lr] + (p - s->off[lr]) * w + (pc - s->off[lr]);
+            } else if (lc == lr - 1) {
+                cidx[cf[p]] = (int32_t)(pc - s->off[lc]);
+                csrc[cf[p]++] = k;
+            } else {
+                uidx[uf[p]] = (int32_t)(pc - s->off[lc]);
+                usrc[uf[p]++] = k;
+                ucrow[ucf[pc]] = (int32_t)(p - s->off[lr]);
+                ucsrc[ucf[pc]++] = k;
+            }
+        }
+    }
+    int rc = upload(&s->perm, perm, "slab perm");
+    if (!rc) rc = upload(&s->dmap, dmap, "slab dmap");
+    if (!rc) rc = upload(&s->cptr, cptr, "slab cptr");
+    if (!rc) rc = upload(&s->cidx, cidx, "slab cidx");
+    if (!rc) rc = upload(&s->csrc, csrc, "slab csrc");
+    if (!rc) rc = upload(&s->uptr, uptr, "slab uptr");
+    if (!rc) rc = upload(&s->uidx, uidx, "slab uidx");
+    if (!rc) rc = upload(&s->usrc, usrc, "slab usrc");
+    if (!rc) rc = upload(&s->ucptr, ucptr, "slab ucptr");
+    if (!rc) rc = upload(&s->ucrow, ucrow, "slab ucrow");
+    if (!rc) rc = upload(&s->ucsrc, ucsrc, "slab ucsrc");
+    if (rc) {
+        slab_free(s);
+        return rc;
+    }
+    *out = s;
+    return EMG_OK;
+}
+
+extern "C" void emg_slab_destroy(emg_slab* s) { slab_free(s); }
+
+extern "C" int emg_slab_info(const emg_slab* s, int64_t* info) {
+    EMG_CHECK_ARG(s && info, "emg_slab_info: NULL argument");
+    info[0] = s->m;
+    info[1] = s->maxw;
+    info[2] = s->totD;
+    info[3] = s->nC;
+    info[4] = s->F;
+    info[5] = s->prec;
+    info[6] = s->n_perturbed;
+    return EMG_OK;
+}
+
+extern "C" int emg_slab_levels(const emg_slab* s, int64_t* off_out, int32_t* perm_out) {
+    EMG_CHECK_ARG(s && off_out, "emg_slab_levels: NULL argument");
+    std::copy(s->off.begin(), s->off.end(), off_out);
+    if (perm_out) EMG_CUDA(cudaMemcpy(perm_out, s->perm, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost));
+    return EMG_OK;
+}
+
+namespace {
+template <typename R>
+int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, const double2* A, cudaStream_t st) {
+    using namespace emg::slab;
+    using T = typename C2<R>::T;
+    slab_free_factors(s);
+    int rc = dalloc(reinterpret_cast<T**>(&s->Sinv), F * s->totD, "slab inverse blocks");
+    if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->Cval), F * std::max<int64_t>(s->nC, 1), "slab C values");
+    if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->Uval), F * std::max<int64_t>(s->nU, 1), "slab U values");
+    if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->UCval), F * std::max<int64_t>(s->nU, 1), "slab U values (by column)");
+    if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->pinv), F * kTile * kTile, "slab pivot tiles");
+    if (!rc) rc = dalloc(&s->perturbed, F, "slab pivot counters");
+    if (rc) { slab_free_factors(s); return rc; }
+    s->F = F;
+    s->prec = sizeof(R) == 4 ? 1 : 2;
+    int32_t* amat = nullptr;
+    rc = dalloc(&amat, F, "slab amat");
+    if (rc) { slab_free_factors(s); return rc; }
+    struct Tmp { int32_t* p; ~Tmp() { if (p) cudaFree(p); } } tmp{amat};
+    EMG_CUDA(cudaMemcpyAsync(amat, amat_h, sizeof(int32_t) * F, cudaMemcpyHostToDevice, st));
+    EMG_CUDA(cudaMemsetAsync(s->perturbed, 0, sizeof(int32_t) * F, st));
+    T* Sinv = static_cast<T*>(s->Sinv);
+    EMG_CUDA(cudaMemsetAsync(Sinv, 0, sizeof(T) * F * s->totD, st));
+    k_values<R><<<grid_for(s->nnz * F, 256), 256, 0, st>>>(s->nnz, Bm, F, amat, A, s->dmap, s->totD, Sinv);
+    if (s->nC)
+        k_offvals<R><<<grid_for(s->nC * F, 256), 256, 0, st>>>(s->nC, Bm, F, amat, A, s->csrc, static_cast<T*>(s->Cval));
+    if (s->nU) {
+        k_offvals<R><<<grid_for(s->nU * F, 256), 256, 0, st>>>(s->nU, Bm, F, amat, A, s->usrc, static_cast<T*>(s->Uval));
+        k_offvals<R><<<grid_for(s->nU * F, 256), 256, 0, st>>>(s->nU, Bm, F, amat, A, s->ucsrc, static_cast<T*>(s->UCval));
+    }
+    EMG_CUDA(cudaGetLastError());
+    const int diag_smem = (int)(sizeof(T) * kTile * (kTile + 1));
+    EMG_CUDA(cudaFuncSetAttribute(k_schur<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSchurSmem));
+    EMG_CUDA(cudaFuncSetAttribute(k_gj_diag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, diag_smem));
+    const R rel_thr = sizeof(R) == 4 ? (R)1e-6 : (R)1e-13;
+    for (int i = 0; i < s->m; ++i) {
+        const int64_t w = s->off[i + 1] - s->off[i];
+        if (i > 0) {
+            const int64_t wp = s->off[i] - s->off[i - 1];
+            const int rb = (int)std::max<int64_t>(1, std::min<int64_t>(kMaxRows, kSchurSmem / (wp * (int64_t)sizeof(T))));
+            const dim3 g((unsigned)((w + rb - 1) / rb), 1, (unsigned)F);
+            k_schur<R><<<g, kThreads, (size_t)rb * wp * sizeof(T), st>>>(
+                wp, w, s->off[i], rb, s->cptr, s->cidx, static_cast<const T*>(s->Cval), s->nC, s->ucptr, s->ucrow,
+                static_cast<const T*>(s->UCval), s->nU, Sinv, s->totD, s->offD[i - 1], s->offD[i]);
+        }
+        const int nt = (int)((w + kTile - 1) / kTile);
+        for (int k = 0; k < nt; ++k) {
+            k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kThreads, diag_smem, st>>>(w, k, Sinv, s->totD, s->offD[i],
+                                                                             static_cast<T*>(s->pinv), rel_thr,
+                                                                             s->perturbed);
+            if (nt > 1) {
+                const T* P = static_cast<const T*>(s->pinv);
+                k_gj_panel<R><<<dim3(nt, 1, (unsigned)F), kThreads, 0, st>>>(0, w, k, Sinv, s->totD, s->offD[i], P);
+                k_gj_panel<R><<<dim3(nt, nt, (unsigned)F), kThreads, 0, st>>>(2, w, k, Sinv, s->totD, s->offD[i], P);
+                k_gj_panel<R><<<dim3(nt, 1, (unsigned)F), kThreads, 0, st>>>(1, w, k, Sinv, s->totD, s->offD[i], P);
+            }
+        }
+        EMG_CUDA(cudaGetLastError());
+    }
+    std::vector<int32_t> pc(F);
+    EMG_CUDA(cudaMemcpyAsync(pc.data(), s->perturbed, sizeof(int32_t) * F, cudaMemcpyDeviceToHost, st));
+    EMG_CUDA(cudaStreamSynchronize(st));
+    s->n_perturbed = 0;
+    for (auto v : pc) s->n_perturbed += v;
+    return EMG_OK;
+}
+}  // namespace
+
+extern "C" int emg_slab_factor(emg_slab* s, int precision, int64_t F, const int32_t* amat, int64_t Bm, const double* A,
+                               void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(s && amat && A && F > 0 && Bm > 0 && (precision == 1 || precision == 2),
+                  "emg_slab_factor: bad argument");
+    for (int64_t f = 0; f < F; ++f) EMG_CHECK_ARG(amat[f] >= 0 && amat[f] < Bm, "emg_slab_factor: amat out of range");
+    if (s->n == 0) return EMG_OK;
+    const auto* Ad = reinterpret_cast<const double2*>(A);
+    return precision == 1 ? slab_factor_t<float>(s, F, amat, Bm, Ad, (cudaStream_t)stream)
+                          : slab_factor_t<double>(s, F, amat, Bm, Ad, (cudaStream_t)stream);
+}
+
+namespace {
+// The slab solve as a GMRES preconditioner: column c uses factor cfac[c].
+struct SlabPrecond : emg::Precond {
+    emg_slab* s;
+    std::vector<int32_t> cfac;
+    std::vector<emg::slab::Group> groups;
+    int64_t Bc = 0;
+    SlabPrecond(emg_slab* s_, int64_t Bc_, const int32_t* cfac_) : s(s_), cfac(cfac_, cfac_ + Bc_), Bc(Bc_) {
+        for (int64_t c = 0; c < Bc; ++c) {
+            if (!groups.empty() && groups.back().fac == cfac[c] && groups.back().col0 + groups.back().ncol == c)
+                groups.back().ncol++;
+            else
+                groups.push_back({cfac[c], (int32_t)c, 1, 0});
+        }
+    }
+    int prepare(int64_t bc) override {
+        using namespace emg;
+        const size_t esz = s->prec == 1 ? sizeof(float2) : sizeof(double2);
+        if (bc > s->ws_cols || !s->Y) {
+            dfree(s->Y); dfree(s->Z); dfree(s->colfac);
+            s->ws_cols = 0;
+            EMG_CUDA(cudaMalloc(&s->Y, esz * s->n * bc));
+            EMG_CUDA(cudaMalloc(&s->Z, esz * s->n * bc));
+            int rc = dalloc(&s->colfac, bc, "slab colfac");
+            if (rc) return rc;
+            s->ws_cols = bc;
+        }
+        if ((int64_t)groups.size() > s->ngroups_cap) {
+            dfree(s->groups);
+            int rc = dalloc(&s->groups, (int64_t)groups.size(), "slab groups");
+            if (rc) return rc;
+            s->ngroups_cap = (int64_t)groups.size();
+        }
+        EMG_CUDA(cudaMemcpy(s->colfac, cfac.data(), sizeof(int32_t) * bc, cudaMemcpyHostToDevice));
+        EMG_CUDA(cudaMemcpy(s->groups, groups.data(), sizeof(emg::slab::Group) * groups.size(), cudaMemcpyHostToDevice));
+        return EMG_OK;
+    }
+    template <typename R>
+    int run(const double2* in, double2* out, cudaStream_t st) {
+        using namespace emg::slab;
+        using T = typename C2<R>::T;
+        T* Y = static_cast<T*>(s->Y);
+        T* Z = static_cast<T*>(s->Z);
+        const T* Sinv = static_cast<const T*>(s->Sinv);
+        const T* Cv = static_cast<const T*>(s->Cval);
+        const T* Uv = static_cast<const T*>(s->Uval);
+        const unsigned G = (unsigned)groups.size();
+        k_gather<R><<<grid_for(s->n * Bc, 256), 256, 0, st>>>(s->n, Bc, s->perm, in, Y);
+        for (int i = 0; i < s->m; ++i) {
+            const int64_t w = s->off[i + 1] - s->off[i];
+            if (i > 0)
+                k_couple<R><<<grid_for(w * Bc, 256), 256, 0, st>>>(0, w, s->off[i], s->off[i - 1], Bc, s->colfac, s->cptr,
+                                                                   s->cidx, Cv, s->nC, Z, Y);
+            k_rowmv<R><<<dim3((unsigned)((w * 32 + kThreads - 1) / kThreads), G), kThreads, 0, st>>>(
+                w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, (R)1, 0, Z);
+        }
+        for (int i = s->m - 2; i >= 0; --i) {
+            const int64_t w = s->off[i + 1] - s->off[i];
+            k_couple<R><<<grid_for(w * Bc, 256), 256, 0, st>>>(1, w, s->off[i], s->off[i + 1], Bc, s->colfac, s->uptr,
+                                                               s->uidx, Uv, s->nU, Z, Y);
+            k_rowmv<R><<<dim3((unsigned)((w * 32 + kThreads - 1) / kThreads), G), kThreads, 0, st>>>(
+                w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, (R)-1, 1, Z);
+        }
+        k_scatter<R><<<grid_for(s->n * Bc, 256), 256, 0, st>>>(s->n, Bc, s->perm, Z, out);
+        EMG_CUDA(cudaGetLastError());
+        return EMG_OK;
+    }
+    int apply(const double2* in, double2* out, cudaStream_t st) override {
+        return s->prec == 1 ? run<float>(in, out, st) : run<double>(in, out, st);
+    }
+};
+}  // namespace
+
+extern "C" int emg_slab_apply(emg_slab* s, int64_t Bc, const int32_t* cfac, const double* X_in, double* X_out,
+                              void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(s && cfac && X_in && X_out && Bc > 0 && X_in != X_out, "emg_slab_apply: bad argument");
+    EMG_CHECK_ARG(s->F > 0, "emg_slab_apply: no factorization");
+    for (int64_t c = 0; c < Bc; ++c) EMG_CHECK_ARG(cfac[c] >= 0 && cfac[c] < s->F, "emg_slab_apply: cfac out of range");
+    if (s->n == 0) return EMG_OK;
+    SlabPrecond M(s, Bc, cfac);
+    int rc = M.prepare(Bc);
+    if (rc) return rc;
+    return M.apply(reinterpret_cast<const double2*>(X_in), reinterpret_cast<double2*>(X_out), (cudaStream_t)stream);
+}
+
+extern "C" int emg_gmres_slab(const emg_rplan* pc, emg_slab* s, int64_t Bc, const int32_t* cmat, int64_t Bm,
+                              const double* A, const int32_t* cfac, const double* rhs, double* x, int restart,
+                              int max_iter, double tol, int32_t* iters_out, double* resid_out, void* stream) {
+    using namespace emg;
+    emg_rplan* p = const_cast<emg_rplan*>(pc);
+    EMG_CHECK_ARG(p && s && s->rp == p && cmat && A && cfac && rhs && x && iters_out && resid_out && Bc > 0 && Bm > 0,
+                  "emg_gmres_slab: bad argument");
+    EMG_CHECK_ARG(restart >= 1 && restart <= 256 && max_iter >= 1 && tol > 0, "emg_gmres_slab: restart must be in [1, 256]");
+    EMG_CHECK_ARG(s->F > 0, "emg_gmres_slab: no factorization");
+    for (int64_t c = 0; c < Bc; ++c) EMG_CHECK_ARG(cfac[c] >= 0 && cfac[c] < s->F, "emg_gmres_slab: cfac out of range");
+    SlabPrecond M(s, Bc, cfac);
+    return gmres_run(p, Bc, cmat, Bm, reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(rhs),
+                     reinterpret_cast<double2*>(x), restart, max_iter, tol, iters_out, resid_out, (cudaStream_t)stream, M,
+                     true);
+}

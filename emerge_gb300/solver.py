@@ -114,26 +114,105 @@ class RestrictedSystem:
         return x, its.cpu().numpy(), res.cpu().numpy()
 
 
-class GPUSolver:
-    """``Solver`` for the reference SolveRoutine (fem/solver.py:117-131): GPU ILU(0)-GMRES.
+class SlabFactor:
+    """Block-tridiagonal ("slab") factorizations of a RestrictedSystem (emg_slab).
 
-    ``A`` arrives restricted (CSC/CSR, complex), ``b`` restricted.  The pattern
-    analysis is cached across calls with the same pattern (every frequency of a
-    sweep); with ``reuse_factorization`` the previous ILU factors are reused
-    (the second port of the same frequency, emfreq3d.py:686-697).
+    Breadth-first level sets of the restricted pattern make A block tridiagonal;
+    ``factor`` stores the dense inverses of the slab Schur complements of F
+    matrices at once, in complex FP32 (``"fp32"``) or FP64 (``"fp64"``).
+    """
+
+    def __init__(self, sysr: RestrictedSystem):
+        self.sys = sysr
+        self._lib = sysr._lib
+        h = ctypes.c_void_p()
+        _lib.call("emg_slab_create", sysr._plan, _stream(), ctypes.byref(h))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._lib.emg_slab_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def info(self) -> dict:
+        v = np.zeros(7, dtype=np.int64)
+        _lib.call("emg_slab_info", self._h, v.ctypes.data_as(ctypes.c_void_p))
+        return {"slabs": int(v[0]), "max_width": int(v[1]), "dense_entries": int(v[2]), "couplings": int(v[3]),
+                "factors": int(v[4]), "precision": {0: None, 1: "fp32", 2: "fp64"}[int(v[5])],
+                "perturbed_pivots": int(v[6])}
+
+    def levels(self):
+        """(slab boundaries (slabs+1), restricted index of each slab position)."""
+        m = self.info()["slabs"]
+        off = np.zeros(m + 1, dtype=np.int64)
+        perm = np.zeros(self.sys.n, dtype=np.int32)
+        _lib.call("emg_slab_levels", self._h, off.ctypes.data_as(ctypes.c_void_p), perm.ctypes.data_as(ctypes.c_void_p))
+        return off, perm
+
+    def factor(self, A: torch.Tensor, amat, precision: str = "fp32") -> None:
+        """Factor the matrices A[:, amat[f]] (A: (nnz_r, Bm) from RestrictedSystem.form)."""
+        am = np.ascontiguousarray(amat, dtype=np.int32)
+        A = A.contiguous()
+        _lib.call("emg_slab_factor", self._h, {"fp32": 1, "fp64": 2}[precision], int(am.size),
+                  am.ctypes.data_as(ctypes.c_void_p), int(A.shape[1]), _vp(A), _stream())
+
+    def apply(self, X: torch.Tensor, cfac) -> torch.Tensor:
+        """A_f^-1 X column by column (X: (n, Bc) complex128), f = cfac[c]."""
+        cf = np.ascontiguousarray(cfac, dtype=np.int32)
+        X = X.contiguous()
+        Y = torch.empty_like(X)
+        _lib.call("emg_slab_apply", self._h, int(X.shape[1]), cf.ctypes.data_as(ctypes.c_void_p), _vp(X), _vp(Y),
+                  _stream())
+        return Y
+
+    def gmres(self, A, rhs, cmat, cfac, x0=None, restart=40, max_iter=2000, tol=1e-10):
+        """FGMRES on column c of rhs with matrix cmat[c], preconditioned by factor cfac[c]."""
+        sysr = self.sys
+        Bc = int(rhs.shape[1])
+        cf = np.ascontiguousarray(cfac, dtype=np.int32)
+        rhs = rhs.contiguous()
+        A = A.contiguous()
+        x = torch.zeros(rhs.shape, dtype=rhs.dtype, device=rhs.device) if x0 is None else x0.contiguous().clone()
+        its = torch.zeros(Bc, dtype=torch.int32, device=sysr.device)
+        res = torch.zeros(Bc, dtype=torch.float64, device=sysr.device)
+        _lib.call("emg_gmres_slab", sysr._plan, self._h, Bc, _vp(cmat), int(A.shape[1]), _vp(A),
+                  cf.ctypes.data_as(ctypes.c_void_p), _vp(rhs), _vp(x), int(restart), int(max_iter),
+                  ctypes.c_double(tol), _vp(its), _vp(res), _stream())
+        return x, its.cpu().numpy(), res.cpu().numpy()
+
+
+class GPUSolver:
+    """``Solver`` for the reference SolveRoutine (fem/solver.py:117-131) on the GPU.
+
+    ``A`` arrives restricted (CSC/CSR, complex), ``b`` restricted.  ``method``:
+    ``"slab"`` (default) — slab factorization in complex FP64 + FGMRES, a direct
+    solve like the reference's SuperLU/PARDISO slot; ``"ilu0"`` — level-scheduled
+    ILU(0) + GMRES in FP64.  The pattern analysis is cached across calls with the
+    same pattern (every frequency of a sweep); with ``reuse_factorization`` the
+    previous factors are reused (the second port of the same frequency,
+    emfreq3d.py:686-697).
     """
 
     real_only = False
     req_sorter = False
 
-    def __init__(self, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000, device="cuda"):
+    def __init__(self, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000, device="cuda",
+                 method: str = "slab"):
+        if method not in ("slab", "ilu0"):
+            raise ValueError(f"GPUSolver: unknown method {method!r}")
         self.own_preconditioner = True
+        self.method = method
         self.tol = tol
         self.restart = restart
         self.max_iter = max_iter
         self.device = torch.device(device)
         self._key = None
         self._sys = None
+        self._slab = None
         self._A = None
         self._LU = None
         self.last_iterations = 0
@@ -153,18 +232,27 @@ class GPUSolver:
             indptr = torch.as_tensor(A.indptr.astype(np.int64), device=dev)
             indices = torch.as_tensor(A.indices.astype(np.int32), device=dev)
             self._sys = RestrictedSystem(indptr, indices, A.nnz, np.arange(n))
+            self._slab = SlabFactor(self._sys) if self.method == "slab" else None
             self._key = key
             reuse_factorization = False
         sysr = self._sys
         vals = torch.as_tensor(A.data.astype(np.complex128), device=dev)
         zeros = torch.zeros_like(vals)
-        if not reuse_factorization or self._LU is None:
+        if not reuse_factorization or self._A is None:
             self._A = sysr.form(vals, zeros, [0.0])
-            self._LU = sysr.ilu0(self._A)
+            if self.method == "slab":
+                self._slab.factor(self._A, [0], "fp64")
+            else:
+                self._LU = sysr.ilu0(self._A)
         rhs = torch.as_tensor(np.asarray(b, dtype=np.complex128), device=dev).reshape(1, n)
         r = sysr.gather(rhs)
         cmat = torch.zeros(1, dtype=torch.int32, device=dev)
-        x, its, res = sysr.gmres(self._A, self._LU, r, cmat, restart=self.restart, max_iter=self.max_iter, tol=self.tol)
+        if self.method == "slab":
+            x, its, res = self._slab.gmres(self._A, r, cmat, [0], restart=min(self.restart, 40),
+                                           max_iter=self.max_iter, tol=self.tol)
+        else:
+            x, its, res = sysr.gmres(self._A, self._LU, r, cmat, restart=self.restart, max_iter=self.max_iter,
+                                     tol=self.tol)
         self.last_iterations = int(its[0])
         self.last_residual = float(res[0])
         info = 0 if res[0] <= self.tol * 10 else int(its[0])
@@ -256,8 +344,83 @@ class FrequencySweep:
                     S[f, i, j] = (G[i, f * npo + j] - (self.Pmode[i] if i == j else 0.0)) / self.Pmode[i]
         return S
 
+    def slab(self) -> SlabFactor:
+        """The slab structure of the restricted system (built on first use)."""
+        if getattr(self, "_slab", None) is None:
+            self._slab = SlabFactor(self.sys)
+            self._slab_key = None
+        return self._slab
+
+    def factor_anchors(self, anchors, precision: str = "fp32") -> float:
+        """Slab factorizations of A(k) at the anchor frequencies (cached); returns seconds."""
+        anchors = np.asarray(anchors, dtype=float)
+        key = (tuple(anchors.tolist()), precision)
+        sl = self.slab()
+        if self._slab_key == key:
+            return 0.0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        k0, gam, _ = self._coeffs(anchors)
+        A = self.sys.form(self.E, self.B, k0 ** 2, self.P, gam)
+        sl.factor(A, np.arange(len(anchors)), precision)
+        del A
+        torch.cuda.synchronize()
+        self._slab_key = key
+        return time.perf_counter() - t0
+
+    @staticmethod
+    def default_anchors(freqs, n_anchor: int) -> np.ndarray:
+        """Centres of n_anchor equal sub-bands of [min(freqs), max(freqs)]."""
+        lo, hi = float(np.min(freqs)), float(np.max(freqs))
+        n_anchor = max(1, int(n_anchor))
+        return lo + (np.arange(n_anchor) + 0.5) * (hi - lo) / n_anchor
+
+    def run_anchored(self, freqs, n_anchor: int = 4, anchors=None, precision: str = "fp32", tol: float = 1e-10,
+                     restart: int = 40, max_iter: int = 2000, x0: torch.Tensor | None = None,
+                     chunk: int | None = None) -> SweepResult:
+        """Batched FGMRES sweep preconditioned by slab factorizations at anchor frequencies.
+
+        Every (frequency, port) column runs FP64 FGMRES to ``tol`` on its own A(k),
+        preconditioned by the factor of the nearest anchor; with ``precision="fp32"``
+        the factors and their solves are complex FP32 (mixed precision: FP32 inner,
+        FP64 residuals and updates)."""
+        freqs = np.asarray(freqs, dtype=float)
+        nf, npo = len(freqs), len(self.ports)
+        anchors = self.default_anchors(freqs, n_anchor) if anchors is None else np.asarray(anchors, dtype=float)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t_fac = self.factor_anchors(anchors, precision)
+        k0, gam, beta = self._coeffs(freqs)
+        near = np.argmin(np.abs(freqs[:, None] - anchors[None, :]), axis=1)
+        sysr, sl = self.sys, self.slab()
+        X = torch.zeros((sysr.n, nf * npo), dtype=torch.complex128, device=self.device)
+        its = np.zeros(nf * npo, dtype=np.int64)
+        res = np.zeros(nf * npo)
+        chunk = chunk or nf
+        for f0 in range(0, nf, chunk):
+            f1 = min(nf, f0 + chunk)
+            A = sysr.form(self.E, self.B, k0[f0:f1] ** 2, self.P, gam[:, f0:f1])
+            rhs = self._rhs(beta[:, f0:f1])
+            cmat = torch.arange(f1 - f0, dtype=torch.int32, device=self.device).repeat_interleave(npo)
+            cfac = np.repeat(near[f0:f1], npo)
+            xin = None if x0 is None else x0[:, f0 * npo:f1 * npo]
+            x, it, rs = sl.gmres(A, rhs, cmat, cfac, x0=xin, restart=restart, max_iter=max_iter, tol=tol)
+            X[:, f0 * npo:f1 * npo] = x
+            its[f0 * npo:f1 * npo] = it
+            res[f0 * npo:f1 * npo] = rs
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        S = self._sparams(X, nf, beta)
+        info = {"anchors": anchors, "precision": precision, "factor_seconds": t_fac, **sl.info()}
+        return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X, info)
+
     def run(self, freqs, method: str = "batched", tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
-            x0: torch.Tensor | None = None, chunk: int | None = None) -> SweepResult:
+            x0: torch.Tensor | None = None, chunk: int | None = None, precond: str = "ilu0") -> SweepResult:
+        """``plain``: one frequency at a time, its own preconditioner and solve (both
+        ports together); ``batched``: every column in lockstep (ILU(0)).  ``precond``
+        of the plain method: ``"ilu0"`` (level-scheduled ILU(0) + GMRES) or
+        ``"slab64"`` / ``"slab32"`` (slab factorization of that frequency in complex
+        FP64 / FP32 + FGMRES: a direct solve with FP64 refinement)."""
         freqs = np.asarray(freqs, dtype=float)
         nf, npo = len(freqs), len(self.ports)
         k0, gam, beta = self._coeffs(freqs)
@@ -270,10 +433,17 @@ class FrequencySweep:
         if method == "plain":
             for f in range(nf):
                 A = sysr.form(self.E, self.B, [k0[f] ** 2], self.P, gam[:, f:f + 1])
-                LU = sysr.ilu0(A)
                 rhs = self._rhs(beta[:, f:f + 1])
                 cmat = torch.zeros(npo, dtype=torch.int32, device=self.device)
-                x, it, rs = sysr.gmres(A, LU, rhs, cmat, restart=restart, max_iter=max_iter, tol=tol)
+                if precond == "ilu0":
+                    LU = sysr.ilu0(A)
+                    x, it, rs = sysr.gmres(A, LU, rhs, cmat, restart=restart, max_iter=max_iter, tol=tol)
+                else:
+                    sl = self.slab()
+                    sl.factor(A, [0], {"slab64": "fp64", "slab32": "fp32"}[precond])
+                    self._slab_key = None
+                    x, it, rs = sl.gmres(A, rhs, cmat, np.zeros(npo, dtype=np.int32), restart=min(restart, 40),
+                                         max_iter=max_iter, tol=tol)
                 X[:, f * npo:(f + 1) * npo] = x
                 its[f * npo:(f + 1) * npo] = it
                 res[f * npo:(f + 1) * npo] = rs
@@ -346,22 +516,72 @@ class FrequencySweep:
         X0 = Q @ y.reshape(nf * npo, r).T                                 # (n, nf*np)
         return X0
 
+    def mlp_guess(self, Xs: torch.Tensor, train_freqs, freqs, steps: int = 1500, seed: int = 0):
+        """Initial guesses from the warm-start MLP trained on the converged columns Xs.
+
+        Targets are the coefficients of each training column in the orthonormal basis
+        of span(Xs) (real and imaginary parts, normalised); the network maps
+        (normalised frequency, port) to them.  Returns (X0, final training loss)."""
+        from .mlp import MLP, features
+        Q, _ = torch.linalg.qr(Xs)
+        Q = Q.contiguous()
+        npo = len(self.ports)
+        Y = (Q.conj().T @ Xs).T                                           # (nt*np, r) complex
+        T = torch.cat([Y.real, Y.imag], dim=1).to(torch.float32)
+        scale = T.abs().max().clamp_min(1e-30)
+        T = (T / scale).contiguous()
+        f_lo, f_hi = float(np.min(freqs)), float(np.max(freqs))
+        fn = lambda f: 2 * (np.asarray(f, dtype=float) - f_lo) / max(f_hi - f_lo, 1e-30) - 1   # noqa: E731
+        tf = np.asarray(train_freqs, dtype=float)
+        xt = features(np.repeat(fn(tf), npo), np.tile(np.arange(npo), len(tf)), npo)
+        net = MLP(xt.shape[1], T.shape[1], max_batch=max(64, len(xt)), seed=seed, device=self.device)
+        hist = net.fit(torch.as_tensor(xt), T, steps=steps, lr=3e-3)
+        fq = np.asarray(freqs, dtype=float)
+        xa = features(np.repeat(fn(fq), npo), np.tile(np.arange(npo), len(fq)), npo)
+        P = net.forward(torch.as_tensor(xa)).to(torch.float64) * scale    # (nf*np, 2r)
+        r = Q.shape[1]
+        yc = torch.complex(P[:, :r], P[:, r:])
+        return (Q @ yc.T).contiguous(), hist[-1]
+
     def run_warm(self, freqs, n_train: int = 32, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
-                 chunk: int | None = None) -> SweepResult:
-        """Batched sweep: solve n_train evenly spread points, project every point onto
-        their span for its initial guess, then finish all points with batched GMRES."""
+                 chunk: int | None = None, guess: str = "projection", solver: str = "ilu0", n_anchor: int = 4,
+                 precision: str = "fp32", mlp_steps: int = 1500) -> SweepResult:
+        """Batched sweep: solve n_train evenly spread points, build an initial guess for
+        every point from their span (``guess`` = "projection": minimal residual;
+        "mlp": the warm-start network; "none": zero), then finish all points with
+        batched GMRES.  ``solver``: "ilu0" (batched ILU(0)-GMRES) or "anchored"
+        (FGMRES preconditioned by slab factors at n_anchor anchors, see run_anchored)."""
         freqs = np.asarray(freqs, dtype=float)
         nf, npo = len(freqs), len(self.ports)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         tr = np.unique(np.round(np.linspace(0, nf - 1, min(n_train, nf))).astype(int))
-        first = self.run(freqs[tr], method="batched", tol=tol, restart=restart, max_iter=max_iter, chunk=chunk)
-        X0 = self.project(first.solutions, freqs)
-        rest = self.run(freqs, method="batched", tol=tol, restart=restart, max_iter=max_iter, x0=X0, chunk=chunk)
+        if solver == "anchored":
+            anchors = self.default_anchors(freqs, n_anchor)
+            solve = lambda fr, x0=None: self.run_anchored(fr, anchors=anchors, precision=precision, tol=tol,  # noqa: E731
+                                                           restart=min(restart, 60), max_iter=max_iter, x0=x0,
+                                                           chunk=chunk)
+        else:
+            solve = lambda fr, x0=None: self.run(fr, method="batched", tol=tol, restart=restart,  # noqa: E731
+                                                 max_iter=max_iter, x0=x0, chunk=chunk)
+        first = solve(freqs[tr])
+        mlp_loss = None
+        torch.cuda.synchronize()
+        tg = time.perf_counter()
+        if guess == "mlp":
+            X0, mlp_loss = self.mlp_guess(first.solutions, freqs[tr], freqs, steps=mlp_steps)
+        elif guess == "projection":
+            X0 = self.project(first.solutions, freqs)
+        else:
+            X0 = None
+        torch.cuda.synchronize()
+        t_guess = time.perf_counter() - tg
+        rest = solve(freqs, X0)
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
         info = {"train_points": len(tr), "train_iterations": first.iterations, "train_seconds": first.seconds,
-                "final_seconds": rest.seconds}
+                "guess_seconds": t_guess, "final_seconds": rest.seconds, "guess": guess, "mlp_loss": mlp_loss,
+                "solver": solver, **({k: v for k, v in first.info.items()} if solver == "anchored" else {})}
         return SweepResult(freqs, rest.S, rest.iterations, rest.residuals, secs, rest.solutions, info)
 
 

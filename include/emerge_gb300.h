@@ -168,6 +168,62 @@ int emg_gmres(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_t Bm
               const double* rhs, double* x, int restart, int max_iter, double tol, int32_t* iters_out,
               double* resid_out, void* stream);
 
+/* ------------------------------------------------------- slab solver ---
+ * Direct block-tridiagonal factorization of the restricted system, the
+ * counterpart of the reference's direct solvers (SolverSuperLU / SolverPardiso /
+ * SolverUMFPACK, fem/solver.py:220-309) on guided-wave structures.  Breadth-first
+ * level sets of the restricted pattern ("slabs") make A block tridiagonal; the
+ * factor holds the dense inverses of the slab Schur complements in complex FP32
+ * (precision 1) or FP64 (precision 2).  One emg_slab holds F factorizations at
+ * once (e.g. anchor frequencies of a sweep), built in the same launches. */
+typedef struct emg_slab emg_slab;
+
+/* Slab structure of a restricted plan (host breadth-first search; synchronises
+ * ``stream``).  EMG_ERR_LIMIT if a slab is wider than 12288 DOFs. */
+int emg_slab_create(const emg_rplan* plan, void* stream, emg_slab** slab);
+void emg_slab_destroy(emg_slab* slab);
+/* info[7] (host): slabs, widest slab, dense entries per factor, coupling entries,
+ * factors held, precision, perturbed pivots of the last factorization. */
+int emg_slab_info(const emg_slab* slab, int64_t* info);
+/* HOST outputs: slab boundaries off_out (slabs+1) and, if not NULL, perm_out
+ * (n_solve): restricted index of each slab position. */
+int emg_slab_levels(const emg_slab* slab, int64_t* off_out, int32_t* perm_out);
+/* Factor the F matrices A[:, amat[f]] (A: [nnz_r][Bm] complex, DEVICE; amat: F
+ * HOST int32).  Replaces any factorization held.  Synchronises ``stream``. */
+int emg_slab_factor(emg_slab* slab, int precision, int64_t F, const int32_t* amat, int64_t Bm, const double* A,
+                    void* stream);
+/* X_out = A_f^-1 X_in column by column, f = cfac[c] (HOST int32, Bc); X_in and
+ * X_out are distinct DEVICE [n_solve][Bc] complex arrays. */
+int emg_slab_apply(emg_slab* slab, int64_t Bc, const int32_t* cfac, const double* X_in, double* X_out, void* stream);
+/* Flexible GMRES (FGMRES, restart <= 256) right-preconditioned by the slab
+ * factors: column c solves A[:, cmat[c]] x = rhs with factor cfac[c] (HOST).  The
+ * residual is FP64 throughout; with FP32 factors this is the mixed-precision
+ * solve (FP32 inner, FP64 refinement).  Same outputs as emg_gmres. */
+int emg_gmres_slab(const emg_rplan* plan, emg_slab* slab, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A,
+                   const int32_t* cfac, const double* rhs, double* x, int restart, int max_iter, double tol,
+                   int32_t* iters_out, double* resid_out, void* stream);
+
+/* ------------------------------------------------------ warm-start MLP ---
+ * No counterpart in the reference (a sweep acceleration).  A multilayer
+ * perceptron in_dim -> hidden_layers x hidden (tanh) -> out_dim with BF16
+ * weights and activations, FP32 accumulation on the tensor cores
+ * (mma.sync m16n8k16), FP32 master weights and Adam.  Dimensions are padded to
+ * multiples of 16 internally; batches up to max_batch rows.  x, y, target are
+ * DEVICE float arrays, row-major (batch x dim). */
+typedef struct emg_mlp emg_mlp;
+int emg_mlp_create(int in_dim, int hidden, int hidden_layers, int out_dim, int max_batch, uint64_t seed,
+                   emg_mlp** mlp);
+int64_t emg_mlp_nparam(const emg_mlp* mlp);
+/* HOST copies of the flat FP32 parameters: per layer W (N x K) then b (N). */
+int emg_mlp_get_params(const emg_mlp* mlp, float* host_out);
+int emg_mlp_set_params(emg_mlp* mlp, const float* host_in);
+int emg_mlp_forward(emg_mlp* mlp, int batch, const float* x, float* y, void* stream);
+/* Forward, mean-squared-error loss (*loss_out, DEVICE), backward; an Adam step
+ * when lr > 0; the gradient is copied to grads_out (DEVICE, nparam) if not NULL. */
+int emg_mlp_train_step(emg_mlp* mlp, int batch, const float* x, const float* target, float lr, float* loss_out,
+                       float* grads_out, void* stream);
+void emg_mlp_destroy(emg_mlp* mlp);
+
 /* CSR pattern without any device allocation.  No counterpart in the reference:
  * an addition for callers that cannot call cudaMalloc, e.g. a host application
  * that must not allocate device memory of its own (its memory is owned by

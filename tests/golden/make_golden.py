@@ -19,6 +19,8 @@ Fixtures:
                      vectors, solve_ids, SuperLU field and S-parameters
                      (fem/physics/edm/assembler.py:312-388, fem/solver.py:405-469,
                      fem/physics/edm/emfreq3d.py:607-779)
+  waveguide_abc.npz  the same guide with port 2 replaced by an AbsorbingBoundary:
+                     K row checksums, solve_ids, port vector at 10 GHz
 """
 from __future__ import annotations
 
@@ -262,8 +264,46 @@ def make_waveguide():
     np.savez_compressed(os.path.join(HERE, "waveguide.npz"), **out)
 
 
+def make_waveguide_abc():
+    """WR-90 guide with port 2 replaced by a first-order absorbing boundary
+    (fem/bc.py:254-300, assemble_robin_bc fem/physics/edm/assembler.py:125-144)."""
+    tm, (a, b, L) = waveguide_mesh()
+    m = reference_mesh(tm)
+    field = Nedelec2(m)
+    nT = m.n_tets
+    er = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    ur = er.copy()
+    p1 = ref_bc.RectangularWaveguide(FaceSelection([pm.FACE_YMIN]), 1, cs=CoordinateSystem(
+        Axis(np.array([1.0, 0, 0])), Axis(np.array([0, 0, 1.0])), Axis(np.array([0, -1.0, 0])),
+        np.array([a / 2, 0.0, b / 2])), dims=(a, b))
+    p1.dims = (a, b)
+    abc = ref_bc.AbsorbingBoundary(FaceSelection([pm.FACE_YMAX]))
+    pec = ref_bc.PEC(FaceSelection([pm.FACE_XMIN, pm.FACE_XMAX, pm.FACE_ZMIN, pm.FACE_ZMAX]))
+    asm = ref_assembler.Assembler()
+    f = 10.0e9
+    K, bvec, solve_ids, pvecs = asm.assemble_freq_matrix(field, er, ur, [pec, p1, abc], f, cache_matrices=True)
+    Kc = K.tocsr()
+    n = Kc.shape[0]
+    out = mesh_arrays(m)
+    out["tet_to_field"] = field.tet_to_field.astype(np.int32)
+    out["tri_to_field"] = field.tri_to_field.astype(np.int32)
+    out["dims"] = np.array([a, b, L])
+    out["freq"] = np.float64(f)
+    out["port_tris_1"] = p1._tri_ids.astype(np.int32) if p1._tri_ids is not None else m.get_triangles(p1.tags).astype(np.int32)
+    out["abc_tris"] = m.get_triangles(abc.tags).astype(np.int32)
+    out["pec_tris"] = m.get_triangles(pec.tags).astype(np.int32)
+    out["K_rowsum"] = np.asarray(Kc.sum(axis=1)).ravel()
+    out["K_rowmom"] = Kc @ ((np.arange(n) + 1.0) / n)
+    out["solve_ids"] = solve_ids.astype(np.int32)
+    nz = np.nonzero(pvecs[1])[0]
+    out["pvec_1_idx"] = nz.astype(np.int32)
+    out["pvec_1_val"] = pvecs[1][nz]
+    np.savez_compressed(os.path.join(HERE, "waveguide_abc.npz"), **out)
+    print("waveguide_abc: ok")
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide"]
+    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc"]
     if "tet" in which:
         make_tet_elements()
     if "tri" in which:
@@ -272,3 +312,5 @@ if __name__ == "__main__":
         make_small_assembly()
     if "waveguide" in which:
         make_waveguide()
+    if "abc" in which:
+        make_waveguide_abc()

@@ -91,3 +91,33 @@ def test_waveport_blocks_match_reference(torch_cuda):
         b = bo.cpu().numpy()
         assert np.abs(B - t["B_force"][k]).max() <= 1e-12 * np.abs(t["B_force"][k]).max()
         assert np.abs(b - t["b_force"][k]).max() <= 1e-12 * np.abs(t["b_force"][k]).max()
+
+
+def test_absorbing_boundary_matrix_matches_reference(torch_cuda):
+    """WR-90 guide with an AbsorbingBoundary on the far end (ned2_tri_stiff path)."""
+    from emerge_gb300 import bc as pbc
+    from emerge_gb300 import mesh as pm
+    from emerge_gb300.freq import Assembler
+    from _fixtures import field_from
+    z = load("waveguide_abc.npz")
+    field = field_from(z)
+    a, b, L = (float(v) for v in z["dims"])
+    tag_tris = {(pm.FACE_YMIN,): z["port_tris_1"], (pm.FACE_YMAX,): z["abc_tris"],
+                (pm.FACE_XMIN, pm.FACE_XMAX, pm.FACE_ZMIN, pm.FACE_ZMAX): z["pec_tris"]}
+    field.mesh.get_triangles = lambda tags: np.asarray(tag_tris[tuple(tags)], dtype=np.int64)
+    p1 = pbc.RectangularWaveguide([pm.FACE_YMIN], 1, pbc.CoordinateSystem([1.0, 0, 0], [0, 0, 1.0], [0, -1.0, 0],
+                                                                        [a / 2, 0.0, b / 2]), (a, b))
+    bcs = [pbc.PEC([pm.FACE_XMIN, pm.FACE_XMAX, pm.FACE_ZMIN, pm.FACE_ZMAX]), p1,
+           pbc.AbsorbingBoundary([pm.FACE_YMAX])]
+    nT = field.mesh.n_tets
+    eye = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    K, b, solve_ids, pvs = Assembler().assemble_freq_matrix(field, eye, eye, bcs, float(z["freq"]))
+    n = K.shape[0]
+    scale = np.abs(K).max(axis=1).toarray().ravel()
+    scale[scale == 0] = 1.0
+    assert np.max(np.abs(np.asarray(K.sum(axis=1)).ravel() - z["K_rowsum"]) / scale) <= TOL
+    assert np.max(np.abs(K @ ((np.arange(n) + 1.0) / n) - z["K_rowmom"]) / scale) <= TOL
+    assert np.array_equal(solve_ids, z["solve_ids"])
+    ref = np.zeros(n, dtype=np.complex128)
+    ref[z["pvec_1_idx"]] = z["pvec_1_val"]
+    assert np.max(np.abs(pvs[1] - ref)) <= TOL * np.max(np.abs(ref))
