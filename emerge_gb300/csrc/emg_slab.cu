@@ -416,6 +416,7 @@ struct Group {
 // Out[r, cols of group g] = beta Out + alpha S_i^-1[r, :] Y[:, cols]: warp per row,
 // lanes over the row of S_i^-1 (coalesced), 16 columns per pass.  Grid: row blocks x groups.
 constexpr int kRowCols = 16;
+constexpr int kWideGroup = 48;     // groups at least this wide use the tiled product
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_rowmv(int64_t w, int64_t row0, int64_t Bc, const Group* __restrict__ groups,
                                                     const typename C2<R>::T* __restrict__ Sinv, int64_t totD, int64_t offD,
@@ -462,6 +463,41 @@ __global__ void __launch_bounds__(kThreads) k_rowmv(int64_t w, int64_t row0, int
     }
 }
 
+// The same product for wide groups: 64 x 64 output tiles through tile_mac.
+// Grid: column tiles x row tiles x groups.
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_slab_gemm(int64_t w, int64_t row0, int64_t Bc,
+                                                        const Group* __restrict__ groups,
+                                                        const typename C2<R>::T* __restrict__ Sinv, int64_t totD,
+                                                        int64_t offD, const typename C2<R>::T* __restrict__ Y, R alpha,
+                                                        int beta, typename C2<R>::T* __restrict__ Out) {
+    using T = typename C2<R>::T;
+    __shared__ Tile<R> sm;
+    const Group g = groups[blockIdx.z];
+    const int64_t c0 = (int64_t)blockIdx.x * kTile, r0 = (int64_t)blockIdx.y * kTile;
+    if (c0 >= g.ncol) return;
+    const int nr = (int)min((int64_t)kTile, w - r0), nc = (int)min((int64_t)kTile, (int64_t)g.ncol - c0);
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
+    tile_mac<R>(acc, Sinv + (int64_t)g.fac * totD + offD + r0 * w, w, Y + row0 * Bc + g.col0 + c0, Bc, nr, nc, w, sm);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = ty + 16 * i, c = tx + 16 * j;
+            if (r < nr && c < nc) {
+                T& o = Out[(row0 + r0 + r) * Bc + g.col0 + c0 + c];
+                const T res = mk(alpha * acc[i][j].x, alpha * acc[i][j].y);
+                if (beta) { o.x += res.x; o.y += res.y; }
+                else o = res;
+            }
+        }
+}
+
 }  // namespace slab
 }  // namespace emg
 
@@ -488,6 +524,7 @@ struct emg_slab {
     int64_t n_perturbed = 0;
     // solve workspace
     int64_t ws_cols = 0;
+    size_t ws_bytes = 0;
     void *Y = nullptr, *Z = nullptr;
     int32_t* colfac = nullptr;
     emg::slab::Group* groups = nullptr;
@@ -786,15 +823,17 @@ struct SlabPrecond : emg::Precond {
     }
     int prepare(int64_t bc) override {
         using namespace emg;
-        const size_t esz = s->prec == 1 ? sizeof(float2) : sizeof(double2);
-        if (bc > s->ws_cols || !s->Y) {
+        const size_t bytes = (s->prec == 1 ? sizeof(float2) : sizeof(double2)) * (size_t)s->n * (size_t)bc;
+        if (bytes > s->ws_bytes || bc > s->ws_cols || !s->Y) {
             dfree(s->Y); dfree(s->Z); dfree(s->colfac);
             s->ws_cols = 0;
-            EMG_CUDA(cudaMalloc(&s->Y, esz * s->n * bc));
-            EMG_CUDA(cudaMalloc(&s->Z, esz * s->n * bc));
+            s->ws_bytes = 0;
+            EMG_CUDA(cudaMalloc(&s->Y, bytes));
+            EMG_CUDA(cudaMalloc(&s->Z, bytes));
             int rc = dalloc(&s->colfac, bc, "slab colfac");
             if (rc) return rc;
             s->ws_cols = bc;
+            s->ws_bytes = bytes;
         }
         if ((int64_t)groups.size() > s->ngroups_cap) {
             dfree(s->groups);
@@ -816,21 +855,31 @@ struct SlabPrecond : emg::Precond {
         const T* Cv = static_cast<const T*>(s->Cval);
         const T* Uv = static_cast<const T*>(s->Uval);
         const unsigned G = (unsigned)groups.size();
+        int maxcol = 0;
+        for (const auto& g : groups) maxcol = std::max(maxcol, (int)g.ncol);
+        // dense slab product: warp-per-row for narrow groups, 64 x 64 tiles for wide ones
+        auto dense = [&](int64_t w, int64_t i, R alpha, int beta) {
+            if (maxcol >= kWideGroup)
+                k_slab_gemm<R><<<dim3((unsigned)((maxcol + kTile - 1) / kTile), (unsigned)((w + kTile - 1) / kTile), G),
+                                 kThreads, 0, st>>>(w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, alpha,
+                                                    beta, Z);
+            else
+                k_rowmv<R><<<dim3((unsigned)((w * 32 + kThreads - 1) / kThreads), G), kThreads, 0, st>>>(
+                    w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, alpha, beta, Z);
+        };
         k_gather<R><<<grid_for(s->n * Bc, 256), 256, 0, st>>>(s->n, Bc, s->perm, in, Y);
         for (int i = 0; i < s->m; ++i) {
             const int64_t w = s->off[i + 1] - s->off[i];
             if (i > 0)
                 k_couple<R><<<grid_for(w * Bc, 256), 256, 0, st>>>(0, w, s->off[i], s->off[i - 1], Bc, s->colfac, s->cptr,
                                                                    s->cidx, Cv, s->nC, Z, Y);
-            k_rowmv<R><<<dim3((unsigned)((w * 32 + kThreads - 1) / kThreads), G), kThreads, 0, st>>>(
-                w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, (R)1, 0, Z);
+            dense(w, i, (R)1, 0);
         }
         for (int i = s->m - 2; i >= 0; --i) {
             const int64_t w = s->off[i + 1] - s->off[i];
             k_couple<R><<<grid_for(w * Bc, 256), 256, 0, st>>>(1, w, s->off[i], s->off[i + 1], Bc, s->colfac, s->uptr,
                                                                s->uidx, Uv, s->nU, Z, Y);
-            k_rowmv<R><<<dim3((unsigned)((w * 32 + kThreads - 1) / kThreads), G), kThreads, 0, st>>>(
-                w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, (R)-1, 1, Z);
+            dense(w, i, (R)-1, 1);
         }
         k_scatter<R><<<grid_for(s->n * Bc, 256), 256, 0, st>>>(s->n, Bc, s->perm, Z, out);
         EMG_CUDA(cudaGetLastError());

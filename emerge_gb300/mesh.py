@@ -206,6 +206,8 @@ def structured_box(xs: np.ndarray, ys: np.ndarray, zs: np.ndarray,
         cell_tag_fn: optional f(cx, cy, cz) -> int tag per hex (evaluated at hex
             centres before jitter); all six tets of a hex share the tag.
 
+    Tet ``p * n_hex + h`` is Kuhn simplex ``p`` of hex ``h``.
+
     Node index = i + (nx+1)*(j + (ny+1)*k).  Boundary tags FACE_XMIN..FACE_ZMAX.
     """
     xs, ys, zs = (np.asarray(v, dtype=np.float64) for v in (xs, ys, zs))
@@ -241,7 +243,7 @@ def structured_box(xs: np.ndarray, ys: np.ndarray, zs: np.ndarray,
         ab = tuple(u + v for u, v in zip(a, unit[p[1]]))
         tets.append(np.stack([v000, nid(I + a[0], J + a[1], K + a[2]),
                               nid(I + ab[0], J + ab[1], K + ab[2]), nid(I + 1, J + 1, K + 1)]))
-    tets = np.stack(tets, axis=1).reshape(4, -1)                   # hex-major, 6 tets per hex
+    tets = np.stack(tets, axis=1).reshape(4, -1)                   # tet p * n_hex + hex (permutation-major)
     # positive orientation (as gmsh emits): EMerge's field interpolation evaluates the
     # barycentrics with |V| (fem/mth/tet.py:371-497) and so assumes det > 0
     p = nodes[:, tets]                                             # (3, 4, nT)
@@ -252,7 +254,7 @@ def structured_box(xs: np.ndarray, ys: np.ndarray, zs: np.ndarray,
         cx = 0.5 * (xs[I] + xs[I + 1])
         cy = 0.5 * (ys[J] + ys[J + 1])
         cz = 0.5 * (zs[K] + zs[K + 1])
-        cell_tag = np.repeat(np.asarray(cell_tag_fn(cx, cy, cz), dtype=np.int64), 6)
+        cell_tag = np.tile(np.asarray(cell_tag_fn(cx, cy, cz), dtype=np.int64), 6)   # same layout as tets
     else:
         cell_tag = None
 

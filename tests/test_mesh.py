@@ -65,3 +65,29 @@ def test_boundary_tags_cover_the_surface():
     m = unit_cube(3)
     bnd = m.get_triangles([1, 2, 3, 4, 5, 6])
     assert len(np.unique(bnd)) == len(bnd) == (m.tri_to_tet[1] < 0).sum()
+
+
+def test_cell_tags_follow_their_hexes():
+    """Every tet carries the tag of the hex it was cut from (tagged by hex centre)."""
+    from emerge_gb300.mesh import structured_box
+    xs = np.array([0.0, 1.0, 2.0, 3.0])
+    ys = np.array([0.0, 0.5, 1.5])
+    zs = np.array([0.0, 1.0, 2.0])
+    box = structured_box(xs, ys, zs, cell_tag_fn=lambda cx, cy, cz: ((cx > 1.0) & (cx < 2.0) & (cz < 1.0)).astype(int))
+    c = box.nodes[:, box.tets].mean(axis=1)
+    inside = (c[0] > 1.0) & (c[0] < 2.0) & (c[2] < 1.0)
+    assert np.array_equal(box.cell_tag == 1, inside)
+    assert box.cell_tag.sum() == 6 * 2    # one x-cell x two y-cells x one z-cell, 6 tets each
+
+
+def test_iris_filter_keeps_only_apertures_in_iris_slabs():
+    from emerge_gb300.geometry import IRIS_APERTURES, iris_filter
+    p = iris_filter(3e-3)
+    c = p.mesh.nodes[:, p.mesh.tets].mean(axis=1)
+    a = 0.02286
+    y = 10e-3
+    for i, w in enumerate(IRIS_APERTURES):
+        sel = (c[1] > y) & (c[1] < y + 2e-3)
+        assert sel.any()
+        assert np.all(c[0, sel] > (a - w) / 2) and np.all(c[0, sel] < (a + w) / 2)
+        y += 2e-3 + ([15.8e-3, 17.6e-3, 18.0e-3, 17.6e-3, 15.8e-3] + [0.0])[i]

@@ -136,3 +136,20 @@ def test_anchored_sweep_matches_reference_sparams(torch_cuda):
     assert np.all(plain.residuals <= 1e-9)
     assert np.max(np.abs(plain.S - z["S"])) <= 1e-4
     assert np.max(np.abs(res.S - plain.S)) <= 1e-7
+
+
+def test_wide_column_groups_use_tiled_product(system):
+    """Groups of >= 48 columns take the 64 x 64 tiled product; same result as narrow groups."""
+    torch, sysr, slab, Ks, rhs, vals = system
+    slab.factor(vals, [0, 1], "fp64")
+    rng = np.random.default_rng(5)
+    n = Ks[0].shape[0]
+    B = rng.standard_normal((n, 70)) + 1j * rng.standard_normal((n, 70))
+    Bt = torch.as_tensor(B, device="cuda")
+    wide = slab.apply(Bt, [0] * 60 + [1] * 10).cpu().numpy()
+    narrow = np.concatenate([slab.apply(Bt[:, c0:c0 + 10], [0] * 10 if c0 < 60 else [1] * 10).cpu().numpy()
+                             for c0 in range(0, 70, 10)], axis=1)
+    assert np.max(np.abs(wide - narrow)) <= 1e-9 * np.max(np.abs(narrow))
+    for c in (0, 59, 65):
+        ref = spla.spsolve(Ks[0 if c < 60 else 1].tocsc(), B[:, c])
+        assert np.linalg.norm(wide[:, c] - ref) / np.linalg.norm(ref) <= 1e-9
