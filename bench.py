@@ -271,12 +271,22 @@ def run_gpu(args, rank, world):
 
 
 def run_sweep(args):
-    """Frequency sweep of the iris filter: batched + warm-started vs plain, both on the GPU.
+    """Iris-filter sweep: batched + mixed-precision + MLP-warm-started vs the plain FP64 GPU solve.
 
-    freq-pts/s = points / wall time of the solve phase (matrices assembled before).
-    The plain method solves one frequency at a time (its own ILU(0), GMRES); it is
-    timed on ``--sweep-plain`` evenly spread points and its rate extrapolated.
-    max|dS| compares the warm-started sweep with the plain solves on those points.
+    freq-pts/s = points / wall time of the solve phase (volume and port matrices
+    assembled before; both methods form A(k) themselves).
+      plain  — one frequency at a time: slab factorization of A(k) in complex FP64 +
+               FGMRES (a direct solve: 1-2 iterations), both ports together; timed
+               on ``--sweep-plain`` points spread over the band, rate extrapolated.
+      fast   — all points: FP32 slab factors at ``--sweep-anchors`` anchor
+               frequencies (one batched factorization), the first ``--sweep-train``
+               points solved by batched FGMRES, the BF16 tensor-core MLP trained on
+               them supplies every point's initial guess, then batched FGMRES on all
+               columns to the same FP64 residual tolerance.
+    max|dS| compares fast with plain on the plain points.  Also reported: the same
+    anchored sweep without a warm start (what the learned guess saves), the
+    ILU(0)-GMRES plain method on one point with capped iterations, and SciPy's
+    SuperLU (the reference's default direct solver) per point on the host cores.
     """
     import torch
     from emerge_gb300.freq import Assembler
@@ -287,29 +297,87 @@ def run_sweep(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sw = FrequencySweep(asm, p.field, p.er, p.ur, p.bcs)
+    sl = sw.slab()
     torch.cuda.synchronize()
     setup = time.perf_counter() - t0
     nf = args.sweep_points
     freqs = np.linspace(8e9, 12e9, nf)
-    idx = np.unique(np.linspace(0, nf - 1, args.sweep_plain).astype(int))
+    idx = np.unique(np.linspace(0, nf - 1, args.sweep_plain + 2).astype(int)[1:-1])
+    chunk = args.sweep_chunk or None
+    out = {"workload": f"{p.name}: N={p.field.n_field} DOFs ({sw.sys.n} after PEC), {nf} points 8-12 GHz x 2 ports",
+           "metric": "sweep freq-pts/s", "tol": args.sweep_tol, "setup_s": round(setup, 2),
+           "slabs": sl.info()["slabs"], "max_slab_width": sl.info()["max_width"]}
     with ClockSampler(0) as clk:
-        warm = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), tol=args.sweep_tol)
-        plain = sw.run(freqs[idx], method="plain", tol=args.sweep_tol)
-    v_warm = nf / warm.seconds
+        # warm-up of every code path on a tiny sweep (graph capture, cuBLAS/cuSOLVER handles)
+        sw.run_warm(freqs[:4], n_train=2, solver="anchored", n_anchor=1, precision="fp32", guess="mlp",
+                    tol=args.sweep_tol, mlp_steps=50)
+        sw._slab_key = None
+        fast = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored", n_anchor=args.sweep_anchors,
+                           precision="fp32", guess="mlp", tol=args.sweep_tol, restart=args.sweep_restart,
+                           chunk=chunk, mlp_steps=args.sweep_mlp_steps)
+        cold = sw.run_anchored(freqs, n_anchor=args.sweep_anchors, precision="fp32", tol=args.sweep_tol,
+                               restart=args.sweep_restart, chunk=chunk)
+        plain = sw.run(freqs[idx], method="plain", precond="slab64", tol=args.sweep_tol)
+    v_fast = nf / fast.seconds
     v_plain = len(idx) / plain.seconds
-    dS = float(np.max(np.abs(warm.S[idx] - plain.S)))
-    return {
-        "workload": f"{p.name}: N={p.field.n_field} DOFs ({sw.sys.n} after PEC), {nf} points 8-12 GHz x 2 ports",
-        "metric": "sweep freq-pts/s", "batched_warm": v_warm, "plain": v_plain, "ratio": v_warm / v_plain,
-        "max_abs_dS_vs_plain": dS, "tol": args.sweep_tol, "setup_s": round(setup, 2),
-        "warm_seconds": round(warm.seconds, 2), "train_points": warm.info["train_points"],
-        "train_seconds": round(warm.info["train_seconds"], 2),
-        "iterations_warm_mean": float(warm.iterations.mean()), "iterations_warm_max": int(warm.iterations.max()),
-        "iterations_train_max": int(np.max(warm.info["train_iterations"])),
-        "iterations_plain_mean": float(plain.iterations.mean()), "plain_points_timed": int(len(idx)),
-        "ilu_levels": sw.sys.levels, "clocks": clk.summary(),
-        "S21_db_samples": [round(float(20 * np.log10(abs(v) + 1e-300)), 2) for v in warm.S[::max(1, nf // 8), 1, 0]],
-    }
+    out.update({
+        "fast": v_fast, "plain": v_plain, "ratio": v_fast / v_plain,
+        "max_abs_dS_vs_plain": float(np.max(np.abs(fast.S[idx] - plain.S))),
+        "max_residual_fast": float(fast.residuals.max()), "max_residual_plain": float(plain.residuals.max()),
+        "fast_seconds": round(fast.seconds, 3), "plain_seconds_per_point": round(plain.seconds / len(idx), 3),
+        "plain_points_timed": int(len(idx)), "anchors": args.sweep_anchors, "precision_inner": "complex fp32",
+        "factor_seconds": round(float(fast.info.get("factor_seconds", 0.0)), 3),
+        "train_points": int(fast.info["train_points"]), "train_seconds": round(fast.info["train_seconds"], 3),
+        "mlp_seconds": round(fast.info["guess_seconds"], 3), "mlp_loss": fast.info["mlp_loss"],
+        "final_seconds": round(fast.info["final_seconds"], 3),
+        "iterations_fast_mean": float(fast.iterations.mean()), "iterations_fast_max": int(fast.iterations.max()),
+        "iterations_cold_mean": float(cold.iterations.mean()), "cold_pts_per_s": nf / cold.seconds,
+        "max_abs_dS_cold_vs_fast": float(np.max(np.abs(cold.S - fast.S))),
+        "iterations_plain_mean": float(plain.iterations.mean()),
+        "S21_db_samples": [round(float(20 * np.log10(abs(v) + 1e-300)), 2) for v in fast.S[::max(1, nf // 8), 1, 0]],
+        "clocks": clk.summary(),
+    })
+    if args.sweep_ilu_iters > 0:
+        ilu = sw.run(freqs[idx[:1]], method="plain", precond="ilu0", tol=args.sweep_tol, max_iter=args.sweep_ilu_iters)
+        out["ilu0_plain_probe"] = {"points": 1, "max_iter": args.sweep_ilu_iters,
+                                   "iterations": int(ilu.iterations.max()), "residual": float(ilu.residuals.max()),
+                                   "seconds": round(ilu.seconds, 2),
+                                   "converged": bool(ilu.residuals.max() <= args.sweep_tol * 10)}
+    if args.sweep_cpu > 0:
+        out["cpu_superlu"] = cpu_superlu(sw, freqs[idx[:args.sweep_cpu]], plain)
+    return out
+
+
+def cpu_superlu(sw, freqs, plain):
+    """SciPy SuperLU (the reference's SolverSuperLU) on the host: per point factor + 2-port solve."""
+    import scipy.sparse as sps
+    import scipy.sparse.linalg as spla
+    import torch
+    sysr = sw.sys
+    n = sysr.n
+    k0, gam, beta = sw._coeffs(freqs)
+    A = sysr.form(sw.E, sw.B, k0 ** 2, sw.P, gam).cpu().numpy()            # (nnz_r, nf)
+    rhs = sw._rhs(beta).cpu().numpy()                                       # (n, nf*np)
+    ptr_t, ind_t = sysr.pattern()
+    npo = len(sw.ports)
+    t0 = time.perf_counter()
+    err = 0.0
+    from scipy.sparse.csgraph import reverse_cuthill_mckee
+    for f in range(len(freqs)):
+        # SolveRoutine with ReverseCuthillMckee + SolverSuperLU (fem/solver.py:135-151, 243-275)
+        M = sps.csr_matrix((A[:, f], ind_t, ptr_t), shape=(n, n))
+        perm = reverse_cuthill_mckee(M)
+        Ms = sps.csc_matrix(M[perm, :][:, perm])
+        lu = spla.splu(Ms, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.01, options=dict(SymmetricMode=True))
+        Xs = lu.solve(rhs[perm, f * npo:(f + 1) * npo])
+        X = np.empty_like(Xs)
+        X[perm] = Xs
+        S = sw._sparams(torch.as_tensor(X, device=sw.device), 1, beta[:, f:f + 1])
+        err = max(err, float(np.max(np.abs(S[0] - plain.S[f]))))
+    secs = time.perf_counter() - t0
+    return {"value": len(freqs) / secs, "unit": "freq-pts/s", "points": len(freqs), "cores": os.cpu_count(),
+            "kind": "reference", "seconds_per_point": round(secs / len(freqs), 2), "max_abs_dS_vs_gpu_plain": err,
+            "sample": "scipy.sparse.linalg.splu + solve of the same restricted A(k), 2 ports, per point"}
 
 
 def main():
@@ -323,9 +391,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the frequency-sweep measurement")
     ap.add_argument("--sweep-h", type=float, default=3e-3, help="iris-filter mesh size (m)")
-    ap.add_argument("--sweep-points", type=int, default=41)
-    ap.add_argument("--sweep-train", type=int, default=8)
+    ap.add_argument("--sweep-points", type=int, default=401)
+    ap.add_argument("--sweep-train", type=int, default=32)
+    ap.add_argument("--sweep-anchors", type=int, default=8)
+    ap.add_argument("--sweep-restart", type=int, default=40)
+    ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: all)")
+    ap.add_argument("--sweep-mlp-steps", type=int, default=1500)
     ap.add_argument("--sweep-plain", type=int, default=2)
+    ap.add_argument("--sweep-ilu-iters", type=int, default=1000)
+    ap.add_argument("--sweep-cpu", type=int, default=1, help="points solved by SciPy SuperLU on the host")
     ap.add_argument("--sweep-tol", type=float, default=1e-8)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

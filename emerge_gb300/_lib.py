@@ -48,11 +48,12 @@ SIGNATURES = {
     "emg_rplan_scatter": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp]),
     "emg_gmres": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int,
                                  ctypes.c_double, c_vp, c_vp, c_vp]),
-    "emg_slab_create": (ctypes.c_int, [c_vp, c_vp, ctypes.POINTER(c_vp)]),
+    "emg_rplan_pattern": (ctypes.c_int, [c_vp, c_vp, c_vp]),
+    "emg_slab_create": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, ctypes.POINTER(c_vp)]),
     "emg_slab_destroy": (None, [c_vp]),
     "emg_slab_info": (ctypes.c_int, [c_vp, c_vp]),
     "emg_slab_levels": (ctypes.c_int, [c_vp, c_vp, c_vp]),
-    "emg_slab_factor": (ctypes.c_int, [c_vp, ctypes.c_int, c_i64, c_vp, c_i64, c_vp, c_vp]),
+    "emg_slab_factor": (ctypes.c_int, [c_vp, ctypes.c_int, c_i64, c_vp, c_i64, c_vp, ctypes.c_int, c_vp]),
     "emg_slab_apply": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
     "emg_gmres_slab": (ctypes.c_int, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_double, c_vp, c_vp, c_vp]),

@@ -541,6 +541,14 @@ extern "C" int64_t emg_rplan_nnz(const emg_rplan* p) { return p ? p->nnz : -1; }
 extern "C" int64_t emg_rplan_levels(const emg_rplan* p) { return p ? (int64_t)p->lptr.size() - 1 : -1; }
 extern "C" void emg_rplan_destroy(emg_rplan* p) { rplan_free(p); }
 
+extern "C" int emg_rplan_pattern(const emg_rplan* p, int64_t* indptr_out, int32_t* indices_out) {
+    using namespace emg;
+    EMG_CHECK_ARG(p && indptr_out && indices_out, "emg_rplan_pattern: NULL argument");
+    EMG_CUDA(cudaMemcpy(indptr_out, p->rptr, sizeof(int64_t) * (p->ns + 1), cudaMemcpyDeviceToHost));
+    if (p->nnz) EMG_CUDA(cudaMemcpy(indices_out, p->rind, sizeof(int32_t) * p->nnz, cudaMemcpyDeviceToHost));
+    return EMG_OK;
+}
+
 extern "C" int emg_rplan_form(const emg_rplan* p, int64_t Bm, const double* E, const double* B, const double* k2,
                               int64_t n_ports, const double* P, const double* gam, double* A, void* stream) {
     using namespace emg;

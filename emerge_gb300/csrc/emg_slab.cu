@@ -202,6 +202,18 @@ __global__ void __launch_bounds__(kThreads) k_schur(int64_t wp, int64_t w, int64
 
 // In-place inverse of pivot tile k (tb x tb) with partial pivoting inside the tile;
 // the inverse also goes to pinv (ld 64).  Grid 1 x 1 x F.
+//
+// Gauss-Jordan on a 64 x 64 shared tile (padded with the identity when tb < 64),
+// two barriers per pivot.  Thread t owns column t/4 and rows t%4 + 4q.  Step c:
+// (S) swap the pivot row p into row c while forming the scaled pivot row and the
+// old column c; (U) rank-1 update, during which the four lanes owning column c+1
+// pick the next pivot (largest |a_rc| below the diagonal, lowest row on ties)
+// with two shuffles.  The row swaps become one column permutation at the end.
+template <typename T> __device__ __forceinline__ T crecip(T v) {
+    const auto m2 = v.x * v.x + v.y * v.y;
+    return mk(v.x / m2, -v.y / m2);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
                                                       int64_t totD, int64_t offD, typename C2<R>::T* __restrict__ pinv,
@@ -209,102 +221,119 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
     using T = typename C2<R>::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T(*a)[kTile + 1] = reinterpret_cast<T(*)[kTile + 1]>(smem_raw);
-    __shared__ int piv[kTile];
+    __shared__ T rowc[kTile], colc[kTile];
+    __shared__ int piv[kTile], perm[kTile];
     __shared__ int s_p;
+    __shared__ T s_pv;
     __shared__ R s_red[kThreads / 32];
     const int64_t f = blockIdx.z;
     T* M = Sinv + f * totD + offD;
     const int64_t k0 = (int64_t)k * kTile;
     const int tb = (int)min((int64_t)kTile, w - k0);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int j = tid >> 2, rq = tid & 3;
     R mx = 0;
-    for (int idx = tid; idx < tb * tb; idx += kThreads) {
-        const int r = idx / tb, c = idx % tb;
-        const T v = M[(k0 + r) * w + k0 + c];
+    for (int idx = tid; idx < kTile * kTile; idx += kThreads) {
+        const int r = idx / kTile, c = idx % kTile;
+        T v;
+        if (r < tb && c < tb) {
+            v = M[(k0 + r) * w + k0 + c];
+            mx = max(mx, v.x * v.x + v.y * v.y);
+        } else {
+            v = mk((R)(r == c ? 1 : 0), (R)0);
+        }
         a[r][c] = v;
-        mx = max(mx, v.x * v.x + v.y * v.y);
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) s_red[wid] = mx;
     __syncthreads();
+    R thr2 = 0;
+#pragma unroll
+    for (int i = 0; i < kThreads / 32; ++i) thr2 = max(thr2, s_red[i]);
+    thr2 *= rel_thr * rel_thr;   // |pivot|^2 at or below this is replaced
+    // the four lanes owning column c choose its pivot among rows [c, tb)
+    auto find = [&](int c) {
+        const unsigned mask = 0xFu << (lane & 28);
+        R best = -1;
+        int bi = tb;
+        T bv = mk((R)0, (R)0);
+#pragma unroll
+        for (int q = 0; q < kTile / 4; ++q) {
+            const int r = rq + 4 * q;
+            if (r >= c && r < tb) {
+                const T v = a[r][c];
+                const R m2 = v.x * v.x + v.y * v.y;
+                if (m2 > best) { best = m2; bi = r; bv = v; }
+            }
+        }
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+            const R ob = __shfl_xor_sync(mask, best, o);
+            const int oi = __shfl_xor_sync(mask, bi, o);
+            const R ox = __shfl_xor_sync(mask, bv.x, o);
+            const R oy = __shfl_xor_sync(mask, bv.y, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; bv = mk(ox, oy); }
+        }
+        if (rq == 0) {
+            if (!(best > thr2)) {   // also catches a zero column
+                bv = mk(thr2 > 0 ? (R)sqrt(thr2) : (R)1, (R)0);
+                atomicAdd(perturbed + f, 1);
+            }
+            s_p = bi < tb ? bi : c;
+            s_pv = bv;
+            piv[c] = s_p;
+        }
+    };
+    if (j == 0) find(0);
+    __syncthreads();
+    for (int c = 0; c < tb; ++c) {
+        const int p = s_p;
+        const T inv = crecip(s_pv);
+        if (tid < kTile) {
+            const T vp = a[p][tid];
+            if (p != c) a[p][tid] = a[c][tid];
+            rowc[tid] = cmul(vp, inv);
+        } else if (tid < 2 * kTile) {
+            const int r = tid - kTile;
+            colc[r] = r == p ? a[c][c] : a[r][c];
+        }
+        __syncthreads();
+        const T rj = rowc[j];
+#pragma unroll
+        for (int q = 0; q < kTile / 4; ++q) {
+            const int r = rq + 4 * q;
+            T v;
+            if (r == c) {
+                v = j == c ? inv : rj;
+            } else if (j == c) {
+                const T t = cmul(colc[r], inv);
+                v = mk(-t.x, -t.y);
+            } else {
+                v = a[r][j];
+                const T t = cmul(colc[r], rj);
+                v.x -= t.x;
+                v.y -= t.y;
+            }
+            a[r][j] = v;
+        }
+        if (c + 1 < tb && j == c + 1) find(c + 1);
+        __syncthreads();
+    }
     if (tid == 0) {
-        R m2 = 0;
-        for (int i = 0; i < kThreads / 32; ++i) m2 = max(m2, s_red[i]);
-        s_red[0] = m2;
+        for (int c = 0; c < kTile; ++c) perm[c] = c;
+        for (int c = tb - 1; c >= 0; --c) {
+            const int q = piv[c];
+            if (q != c) { const int t = perm[c]; perm[c] = perm[q]; perm[q] = t; }
+        }
     }
     __syncthreads();
-    const R thr2 = s_red[0] * rel_thr * rel_thr;   // |pivot|^2 below this is replaced
-    constexpr int kPer = kTile * kTile / kThreads;
-    T vals[kPer];
-    for (int c = 0; c < tb; ++c) {
-        if (wid == 0) {
-            R best = -1;
-            int bi = c;
-            for (int r = c + lane; r < tb; r += 32) {
-                const R m2 = a[r][c].x * a[r][c].x + a[r][c].y * a[r][c].y;
-                if (m2 > best) { best = m2; bi = r; }
-            }
-#pragma unroll
-            for (int o = 16; o; o >>= 1) {
-                const R ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-            }
-            if (lane == 0) { s_p = bi; piv[c] = bi; }
-        }
-        __syncthreads();
-        const int p = s_p;
-        if (p != c && tid < tb) {
-            const T t = a[p][tid];
-            a[p][tid] = a[c][tid];
-            a[c][tid] = t;
-        }
-        __syncthreads();
-        T pv = a[c][c];
-        R m2 = pv.x * pv.x + pv.y * pv.y;
-        if (!(m2 > thr2)) {   // also catches a zero pivot of an all-zero tile
-            pv = mk(sqrt(thr2) > 0 ? (R)sqrt(thr2) : (R)1, (R)0);
-            m2 = pv.x * pv.x;
-            if (tid == 0) atomicAdd(perturbed + f, 1);
-        }
-        const T inv = mk(pv.x / m2, -pv.y / m2);
-#pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            const int idx = tid + kThreads * q;
-            const int r = idx / kTile, j = idx % kTile;
-            if (r >= tb || j >= tb) continue;
-            T v;
-            if (r == c && j == c) v = inv;
-            else if (r == c) v = cmul(a[c][j], inv);
-            else if (j == c) { const T t = cmul(a[r][c], inv); v = mk(-t.x, -t.y); }
-            else { v = a[r][j]; const T t = cmul(a[r][c], inv); const T u = cmul(t, a[c][j]); v.x -= u.x; v.y -= u.y; }
-            vals[q] = v;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            const int idx = tid + kThreads * q;
-            const int r = idx / kTile, j = idx % kTile;
-            if (r < tb && j < tb) a[r][j] = vals[q];
-        }
-        __syncthreads();
-    }
-    // undo the row interchanges as column interchanges, last first
-    for (int c = tb - 1; c >= 0; --c) {
-        const int p = piv[c];
-        if (p != c && tid < tb) {
-            const T t = a[tid][p];
-            a[tid][p] = a[tid][c];
-            a[tid][c] = t;
-        }
-        __syncthreads();
-    }
     T* P = pinv + f * kTile * kTile;
     for (int idx = tid; idx < tb * tb; idx += kThreads) {
         const int r = idx / tb, c = idx % tb;
-        M[(k0 + r) * w + k0 + c] = a[r][c];
-        P[r * kTile + c] = a[r][c];
+        const T v = a[r][perm[c]];
+        M[(k0 + r) * w + k0 + c] = v;
+        P[r * kTile + c] = v;
     }
 }
 
@@ -363,6 +392,38 @@ __global__ void __launch_bounds__(kThreads) k_gj_panel(int mode, int64_t w, int 
                 if (mode == 0) o = acc[i][j];
                 else if (mode == 1) o = mk(-acc[i][j].x, -acc[i][j].y);
                 else { o.x -= acc[i][j].x; o.y -= acc[i][j].y; }
+            }
+        }
+}
+
+// C = alpha A B + diag I for F batched w x w row-major blocks (batch stride
+// ``stride``; C aliases neither A nor B).  Grid: column tiles x row tiles x F.
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_sq_gemm(int64_t w, const typename C2<R>::T* __restrict__ A,
+                                                      int64_t sA, const typename C2<R>::T* __restrict__ B, int64_t sB,
+                                                      typename C2<R>::T* __restrict__ C, int64_t sC, R alpha, R diag) {
+    using T = typename C2<R>::T;
+    __shared__ Tile<R> sm;
+    const int64_t f = blockIdx.z;
+    const int64_t c0 = (int64_t)blockIdx.x * kTile, r0 = (int64_t)blockIdx.y * kTile;
+    const int nr = (int)min((int64_t)kTile, w - r0), nc = (int)min((int64_t)kTile, w - c0);
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
+    tile_mac<R>(acc, A + f * sA + r0 * w, w, B + f * sB + c0, w, nr, nc, w, sm);
+    T* Cf = C + f * sC;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = ty + 16 * i, c = tx + 16 * j;
+            if (r < nr && c < nc) {
+                T v = mk(alpha * acc[i][j].x, alpha * acc[i][j].y);
+                if (r0 + r == c0 + c) v.x += diag;
+                Cf[(r0 + r) * w + c0 + c] = v;
             }
         }
 }
@@ -557,12 +618,16 @@ int upload(V** d, const std::vector<V>& h, const char* what) {
     return EMG_OK;
 }
 
-// Breadth-first levels over the nodes not yet placed; returns the nodes of the
-// component of ``start`` in level order (lev filled, levels numbered from base).
-std::vector<int64_t> bfs(int64_t start, const std::vector<int64_t>& ptr, const std::vector<int32_t>& ind,
-                         std::vector<int32_t>& lev, int32_t base) {
-    std::vector<int64_t> order{start};
-    lev[start] = base;
+// Breadth-first levels over the nodes not yet placed, from one or more start
+// nodes (all at level ``base``); returns the reached nodes in level order.
+std::vector<int64_t> bfs(const std::vector<int64_t>& starts, const std::vector<int64_t>& ptr,
+                         const std::vector<int32_t>& ind, std::vector<int32_t>& lev, int32_t base) {
+    std::vector<int64_t> order;
+    for (int64_t s : starts)
+        if (lev[s] < 0) {
+            lev[s] = base;
+            order.push_back(s);
+        }
     for (size_t h = 0; h < order.size(); ++h) {
         const int64_t v = order[h];
         for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) {
@@ -577,9 +642,12 @@ std::vector<int64_t> bfs(int64_t start, const std::vector<int64_t>& ptr, const s
 }
 }  // namespace
 
-extern "C" int emg_slab_create(const emg_rplan* rp, void* stream, emg_slab** out) {
+extern "C" int emg_slab_create(const emg_rplan* rp, int64_t n_seeds, const int64_t* seeds, void* stream,
+                               emg_slab** out) {
     using namespace emg;
-    EMG_CHECK_ARG(rp && out, "emg_slab_create: NULL argument");
+    EMG_CHECK_ARG(rp && out && n_seeds >= 0 && (n_seeds == 0 || seeds), "emg_slab_create: NULL argument");
+    for (int64_t i = 0; i < n_seeds; ++i)
+        EMG_CHECK_ARG(seeds[i] >= 0 && seeds[i] < rp->ns, "emg_slab_create: seed out of range");
     *out = nullptr;
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t n = rp->ns, nnz = rp->nnz;
@@ -588,15 +656,22 @@ extern "C" int emg_slab_create(const emg_rplan* rp, void* stream, emg_slab** out
     EMG_CUDA(cudaMemcpyAsync(ptr.data(), rp->rptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st));
     if (nnz) EMG_CUDA(cudaMemcpyAsync(ind.data(), rp->rind, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, st));
     EMG_CUDA(cudaStreamSynchronize(st));
-    // levels: per connected component, BFS from a pseudo-peripheral node (three
-    // sweeps, each restarting from a minimum-degree node of the last level)
+    // levels: the seeds' components by one multi-source BFS from the seeds (e.g. the
+    // DOFs next to one face: planar slabs); every other connected component by BFS
+    // from a pseudo-peripheral node (three sweeps, each restarting from a
+    // minimum-degree node of the last level)
     std::vector<int32_t> lev(n, -1), tmp(n, -1);
     int32_t base = 0;
+    if (n_seeds > 0) {
+        std::vector<int64_t> st0(seeds, seeds + n_seeds);
+        std::vector<int64_t> ord = bfs(st0, ptr, ind, lev, base);
+        for (int64_t v : ord) base = std::max(base, lev[v] + 1);
+    }
     for (int64_t s0 = 0; s0 < n; ++s0) {
         if (lev[s0] >= 0) continue;
         int64_t start = s0;
         for (int sweep = 0; sweep < 3; ++sweep) {
-            std::vector<int64_t> ord = bfs(start, ptr, ind, tmp, 0);
+            std::vector<int64_t> ord = bfs({start}, ptr, ind, tmp, 0);
             const int32_t last = tmp[ord.back()];
             int64_t best = ord.back();
             for (auto it = ord.rbegin(); it != ord.rend() && tmp[*it] == last; ++it)
@@ -606,7 +681,7 @@ extern "C" int emg_slab_create(const emg_rplan* rp, void* stream, emg_slab** out
             for (int64_t v : ord) tmp[v] = -1;
             start = best;
         }
-        std::vector<int64_t> ord = bfs(start, ptr, ind, lev, base);
+        std::vector<int64_t> ord = bfs({start}, ptr, ind, lev, base);
         int32_t top = base;
         for (int64_t v : ord) top = std::max(top, lev[v]);
         base = top + 1;
@@ -728,7 +803,8 @@ extern "C" int emg_slab_levels(const emg_slab* s, int64_t* off_out, int32_t* per
 
 namespace {
 template <typename R>
-int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, const double2* A, cudaStream_t st) {
+int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, const double2* A, int refine,
+                  cudaStream_t st) {
     using namespace emg::slab;
     using T = typename C2<R>::T;
     slab_free_factors(s);
@@ -745,6 +821,15 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
     rc = dalloc(&amat, F, "slab amat");
     if (rc) { slab_free_factors(s); return rc; }
     struct Tmp { int32_t* p; ~Tmp() { if (p) cudaFree(p); } } tmp{amat};
+    // Newton-Schulz scratch: a copy of S_i and the factor 2I - S_i X (F blocks of maxw^2)
+    T *Scopy = nullptr, *Rbuf = nullptr;
+    const int64_t sq = s->maxw * s->maxw;
+    if (refine > 0) {
+        rc = dalloc(&Scopy, F * sq, "slab refinement copy");
+        if (!rc) rc = dalloc(&Rbuf, F * sq, "slab refinement factor");
+        if (rc) { dfree(Scopy); slab_free_factors(s); return rc; }
+    }
+    struct Tmp2 { T* a; T* b; ~Tmp2() { if (a) cudaFree(a); if (b) cudaFree(b); } } tmp2{Scopy, Rbuf};
     EMG_CUDA(cudaMemcpyAsync(amat, amat_h, sizeof(int32_t) * F, cudaMemcpyHostToDevice, st));
     EMG_CUDA(cudaMemsetAsync(s->perturbed, 0, sizeof(int32_t) * F, st));
     T* Sinv = static_cast<T*>(s->Sinv);
@@ -765,13 +850,19 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
         const int64_t w = s->off[i + 1] - s->off[i];
         if (i > 0) {
             const int64_t wp = s->off[i] - s->off[i - 1];
-            const int rb = (int)std::max<int64_t>(1, std::min<int64_t>(kMaxRows, kSchurSmem / (wp * (int64_t)sizeof(T))));
+            // rows per CTA: enough CTAs for two per SM, at most kMaxRows, within shared memory
+            const int64_t rb_grid = std::max<int64_t>(1, (w * F) / (2 * 152));
+            const int rb = (int)std::max<int64_t>(
+                1, std::min<int64_t>({(int64_t)kMaxRows, kSchurSmem / (wp * (int64_t)sizeof(T)), rb_grid}));
             const dim3 g((unsigned)((w + rb - 1) / rb), 1, (unsigned)F);
             k_schur<R><<<g, kThreads, (size_t)rb * wp * sizeof(T), st>>>(
                 wp, w, s->off[i], rb, s->cptr, s->cidx, static_cast<const T*>(s->Cval), s->nC, s->ucptr, s->ucrow,
                 static_cast<const T*>(s->UCval), s->nU, Sinv, s->totD, s->offD[i - 1], s->offD[i]);
         }
         const int nt = (int)((w + kTile - 1) / kTile);
+        if (refine > 0)   // keep S_i for the refinement
+            EMG_CUDA(cudaMemcpy2DAsync(Scopy, sizeof(T) * sq, Sinv + s->offD[i], sizeof(T) * s->totD, sizeof(T) * w * w,
+                                       (size_t)F, cudaMemcpyDeviceToDevice, st));
         for (int k = 0; k < nt; ++k) {
             k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kThreads, diag_smem, st>>>(w, k, Sinv, s->totD, s->offD[i],
                                                                              static_cast<T*>(s->pinv), rel_thr,
@@ -782,6 +873,16 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
                 k_gj_panel<R><<<dim3(nt, nt, (unsigned)F), kThreads, 0, st>>>(2, w, k, Sinv, s->totD, s->offD[i], P);
                 k_gj_panel<R><<<dim3(nt, 1, (unsigned)F), kThreads, 0, st>>>(1, w, k, Sinv, s->totD, s->offD[i], P);
             }
+        }
+        // X <- X (2I - S X): squares the residual I - S X of the inverse.  S_i's copy
+        // is free once 2I - S X is formed and receives the new X.
+        if (refine > 0) {
+            T* X = Sinv + s->offD[i];
+            const dim3 g((unsigned)nt, (unsigned)nt, (unsigned)F);
+            k_sq_gemm<R><<<g, kThreads, 0, st>>>(w, Scopy, sq, X, s->totD, Rbuf, sq, (R)-1, (R)2);
+            k_sq_gemm<R><<<g, kThreads, 0, st>>>(w, X, s->totD, Rbuf, sq, Scopy, sq, (R)1, (R)0);
+            EMG_CUDA(cudaMemcpy2DAsync(X, sizeof(T) * s->totD, Scopy, sizeof(T) * sq, sizeof(T) * w * w, (size_t)F,
+                                       cudaMemcpyDeviceToDevice, st));
         }
         EMG_CUDA(cudaGetLastError());
     }
@@ -795,15 +896,15 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
 }  // namespace
 
 extern "C" int emg_slab_factor(emg_slab* s, int precision, int64_t F, const int32_t* amat, int64_t Bm, const double* A,
-                               void* stream) {
+                               int refine, void* stream) {
     using namespace emg;
-    EMG_CHECK_ARG(s && amat && A && F > 0 && Bm > 0 && (precision == 1 || precision == 2),
+    EMG_CHECK_ARG(s && amat && A && F > 0 && Bm > 0 && (precision == 1 || precision == 2) && refine >= 0 && refine <= 1,
                   "emg_slab_factor: bad argument");
     for (int64_t f = 0; f < F; ++f) EMG_CHECK_ARG(amat[f] >= 0 && amat[f] < Bm, "emg_slab_factor: amat out of range");
     if (s->n == 0) return EMG_OK;
     const auto* Ad = reinterpret_cast<const double2*>(A);
-    return precision == 1 ? slab_factor_t<float>(s, F, amat, Bm, Ad, (cudaStream_t)stream)
-                          : slab_factor_t<double>(s, F, amat, Bm, Ad, (cudaStream_t)stream);
+    return precision == 1 ? slab_factor_t<float>(s, F, amat, Bm, Ad, refine, (cudaStream_t)stream)
+                          : slab_factor_t<double>(s, F, amat, Bm, Ad, refine, (cudaStream_t)stream);
 }
 
 namespace {

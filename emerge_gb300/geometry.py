@@ -9,6 +9,9 @@ and their surfaces made PEC.  All lengths in metres.
 * ``iris_filter`` — five-cavity WR-90 bandpass filter: six inductive irises
   2 mm thick with centred apertures [12.0, 8.5, 7.8, 7.8, 8.5, 12.0] mm, cavity
   lengths [15.8, 17.6, 18.0, 17.6, 15.8] mm, 10 mm feed guides.
+* ``dielectric_cavity`` — PEC box with a centred full-height dielectric cylinder
+  (staircased on the grid), the eigenmode workload; ``cavity_set`` draws a batch
+  of them from a seed.
 """
 from __future__ import annotations
 
@@ -17,7 +20,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from .bc import PEC, CoordinateSystem, RectangularWaveguide
-from .mesh import Nedelec2Basis, TetMesh, structured_box
+from .mesh import FACE_XMAX, FACE_XMIN, FACE_YMAX, FACE_YMIN, FACE_ZMAX, FACE_ZMIN, Nedelec2Basis, TetMesh, structured_box
 
 TAG_PORT1, TAG_PORT2, TAG_PEC = 11, 12, 13
 
@@ -104,3 +107,40 @@ def iris_filter(h: float = 2e-3, a: float = 0.02286, b: float = 0.01016, t: floa
         return m.astype(np.int64)
 
     return _guide_problem(xs, ys, zs, metal, a, b, L, f"5-cavity WR-90 iris filter, h={h * 1e3:.2f} mm")
+
+
+def dielectric_cavity(a: float, b: float, c: float, radius: float, eps_r: float, h: float) -> Problem:
+    """PEC box a x b x c with a centred cylinder (axis z, full height) of permittivity eps_r.
+
+    Cells whose centre lies inside the cylinder carry eps_r (a staircased cylinder);
+    the grid spacing is at most h.  All six faces are PEC; no ports."""
+    xs = _lines([0.0, a], h)
+    ys = _lines([0.0, b], h)
+    zs = _lines([0.0, c], h)
+
+    def inside(cx, cy, cz):
+        return (((cx - a / 2) ** 2 + (cy - b / 2) ** 2) < radius ** 2).astype(np.int64)
+
+    mesh = structured_box(xs, ys, zs, cell_tag_fn=inside)
+    field = Nedelec2Basis(mesh)
+    nT = mesh.n_tets
+    er = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    er[[0, 1, 2], [0, 1, 2], :] = np.where(mesh.cell_tag == 1, eps_r, 1.0)[None, :]
+    ur = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    pec = PEC([FACE_XMIN, FACE_XMAX, FACE_YMIN, FACE_YMAX, FACE_ZMIN, FACE_ZMAX])
+    return Problem(mesh, field, [pec], er, ur,
+                   f"PEC cavity {a * 1e3:.1f}x{b * 1e3:.1f}x{c * 1e3:.1f} mm, cylinder r={radius * 1e3:.2f} mm "
+                   f"eps={eps_r:.2f}, h={h * 1e3:.2f} mm")
+
+
+def cavity_set(n: int = 64, seed: int = 4, h: float = 2e-3):
+    """Seeded batch of dielectric cavities: sides ~ U[15, 40] mm, radius ~ U[2, 6] mm,
+    eps_r ~ U[2, 30] (numpy default_rng(seed)).  Returns a list of Problems."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        a, b, c = rng.uniform(15e-3, 40e-3, 3)
+        r = min(rng.uniform(2e-3, 6e-3), 0.45 * min(a, b))
+        eps = rng.uniform(2.0, 30.0)
+        out.append(dielectric_cavity(a, b, c, r, eps, h))
+    return out

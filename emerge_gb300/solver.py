@@ -60,6 +60,14 @@ class RestrictedSystem:
                 pass
             self._plan = None
 
+    def pattern(self):
+        """Host copy of the restricted CSR pattern (indptr int64, indices int32)."""
+        indptr = np.zeros(self.n + 1, dtype=np.int64)
+        indices = np.zeros(max(self.nnz, 1), dtype=np.int32)
+        _lib.call("emg_rplan_pattern", self._plan, indptr.ctypes.data_as(ctypes.c_void_p),
+                  indices.ctypes.data_as(ctypes.c_void_p))
+        return indptr, indices[: self.nnz]
+
     def form(self, E, B, k2, P=None, gam=None) -> torch.Tensor:
         """Bm restricted matrices (nnz_r, Bm): E - k2[m] B + sum_p gam[p, m] P[p]."""
         k2 = torch.as_tensor(np.ascontiguousarray(k2, dtype=np.float64), device=self.device)
@@ -114,6 +122,26 @@ class RestrictedSystem:
         return x, its.cpu().numpy(), res.cpu().numpy()
 
 
+def dof_positions(field) -> np.ndarray:
+    """(3, n_field) position of every DOF: its edge's midpoint or its face's centroid.
+
+    DOF numbering of Nedelec2 (fem/elements/nedelec2.py:46-50): [edges, faces + nE,
+    edges + nE + nF, faces + 2 nE + nF]."""
+    m = field.mesh
+    nodes = np.asarray(m.nodes)
+    e_mid = nodes[:, np.asarray(m.edges)].mean(axis=1)
+    f_mid = nodes[:, np.asarray(m.tris)].mean(axis=1)
+    return np.concatenate([e_mid, f_mid, e_mid, f_mid], axis=1)
+
+
+def face_seeds(field, solve_ids, axis: int) -> np.ndarray:
+    """Restricted indices of the kept DOFs with the smallest coordinate along ``axis``:
+    the start set of a slab search whose slabs are then cross-sections normal to it."""
+    pos = dof_positions(field)[axis, np.asarray(solve_ids, dtype=np.int64)]
+    lo, hi = float(pos.min()), float(pos.max())
+    return np.flatnonzero(pos <= lo + 1e-9 * max(hi - lo, 1e-30)).astype(np.int64)
+
+
 class SlabFactor:
     """Block-tridiagonal ("slab") factorizations of a RestrictedSystem (emg_slab).
 
@@ -122,11 +150,13 @@ class SlabFactor:
     matrices at once, in complex FP32 (``"fp32"``) or FP64 (``"fp64"``).
     """
 
-    def __init__(self, sysr: RestrictedSystem):
+    def __init__(self, sysr: RestrictedSystem, seeds=None):
         self.sys = sysr
         self._lib = sysr._lib
         h = ctypes.c_void_p()
-        _lib.call("emg_slab_create", sysr._plan, _stream(), ctypes.byref(h))
+        sd = np.ascontiguousarray(np.zeros(0) if seeds is None else seeds, dtype=np.int64)
+        _lib.call("emg_slab_create", sysr._plan, int(sd.size), sd.ctypes.data_as(ctypes.c_void_p) if sd.size else None,
+                  _stream(), ctypes.byref(h))
         self._h = h
 
     def __del__(self):
@@ -153,12 +183,13 @@ class SlabFactor:
         _lib.call("emg_slab_levels", self._h, off.ctypes.data_as(ctypes.c_void_p), perm.ctypes.data_as(ctypes.c_void_p))
         return off, perm
 
-    def factor(self, A: torch.Tensor, amat, precision: str = "fp32") -> None:
-        """Factor the matrices A[:, amat[f]] (A: (nnz_r, Bm) from RestrictedSystem.form)."""
+    def factor(self, A: torch.Tensor, amat, precision: str = "fp32", refine: int = 0) -> None:
+        """Factor the matrices A[:, amat[f]] (A: (nnz_r, Bm) from RestrictedSystem.form);
+        ``refine=1``: one Newton-Schulz step on every slab inverse."""
         am = np.ascontiguousarray(amat, dtype=np.int32)
         A = A.contiguous()
         _lib.call("emg_slab_factor", self._h, {"fp32": 1, "fp64": 2}[precision], int(am.size),
-                  am.ctypes.data_as(ctypes.c_void_p), int(A.shape[1]), _vp(A), _stream())
+                  am.ctypes.data_as(ctypes.c_void_p), int(A.shape[1]), _vp(A), int(refine), _stream())
 
     def apply(self, X: torch.Tensor, cfac) -> torch.Tensor:
         """A_f^-1 X column by column (X: (n, Bc) complex128), f = cfac[c]."""
@@ -345,16 +376,23 @@ class FrequencySweep:
         return S
 
     def slab(self) -> SlabFactor:
-        """The slab structure of the restricted system (built on first use)."""
+        """The slab structure of the restricted system (built on first use).  Slabs are
+        cross-sections of the guide: the search starts from the DOFs on the first
+        port's face."""
         if getattr(self, "_slab", None) is None:
-            self._slab = SlabFactor(self.sys)
+            seeds = None
+            if self.ports:
+                u = self.u[self.ports[0].port_number].abs().cpu().numpy()
+                on_port = np.flatnonzero(u[self.solve_ids] > 0)
+                seeds = on_port if on_port.size else None
+            self._slab = SlabFactor(self.sys, seeds)
             self._slab_key = None
         return self._slab
 
-    def factor_anchors(self, anchors, precision: str = "fp32") -> float:
+    def factor_anchors(self, anchors, precision: str = "fp32", refine: int = 0) -> float:
         """Slab factorizations of A(k) at the anchor frequencies (cached); returns seconds."""
         anchors = np.asarray(anchors, dtype=float)
-        key = (tuple(anchors.tolist()), precision)
+        key = (tuple(anchors.tolist()), precision, refine)
         sl = self.slab()
         if self._slab_key == key:
             return 0.0
@@ -362,7 +400,7 @@ class FrequencySweep:
         t0 = time.perf_counter()
         k0, gam, _ = self._coeffs(anchors)
         A = self.sys.form(self.E, self.B, k0 ** 2, self.P, gam)
-        sl.factor(A, np.arange(len(anchors)), precision)
+        sl.factor(A, np.arange(len(anchors)), precision, refine)
         del A
         torch.cuda.synchronize()
         self._slab_key = key
@@ -377,7 +415,7 @@ class FrequencySweep:
 
     def run_anchored(self, freqs, n_anchor: int = 4, anchors=None, precision: str = "fp32", tol: float = 1e-10,
                      restart: int = 40, max_iter: int = 2000, x0: torch.Tensor | None = None,
-                     chunk: int | None = None) -> SweepResult:
+                     chunk: int | None = None, refine: int = 0) -> SweepResult:
         """Batched FGMRES sweep preconditioned by slab factorizations at anchor frequencies.
 
         Every (frequency, port) column runs FP64 FGMRES to ``tol`` on its own A(k),
@@ -389,7 +427,7 @@ class FrequencySweep:
         anchors = self.default_anchors(freqs, n_anchor) if anchors is None else np.asarray(anchors, dtype=float)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        t_fac = self.factor_anchors(anchors, precision)
+        t_fac = self.factor_anchors(anchors, precision, refine)
         k0, gam, beta = self._coeffs(freqs)
         near = np.argmin(np.abs(freqs[:, None] - anchors[None, :]), axis=1)
         sysr, sl = self.sys, self.slab()
@@ -411,7 +449,7 @@ class FrequencySweep:
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
         S = self._sparams(X, nf, beta)
-        info = {"anchors": anchors, "precision": precision, "factor_seconds": t_fac, **sl.info()}
+        info = {"anchors": anchors, "precision": precision, "refine": refine, "factor_seconds": t_fac, **sl.info()}
         return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X, info)
 
     def run(self, freqs, method: str = "batched", tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
@@ -534,9 +572,9 @@ class FrequencySweep:
         fn = lambda f: 2 * (np.asarray(f, dtype=float) - f_lo) / max(f_hi - f_lo, 1e-30) - 1   # noqa: E731
         tf = np.asarray(train_freqs, dtype=float)
         xt = features(np.repeat(fn(tf), npo), np.tile(np.arange(npo), len(tf)), npo)
-        net = MLP(xt.shape[1], T.shape[1], max_batch=max(64, len(xt)), seed=seed, device=self.device)
-        hist = net.fit(torch.as_tensor(xt), T, steps=steps, lr=3e-3)
         fq = np.asarray(freqs, dtype=float)
+        net = MLP(xt.shape[1], T.shape[1], max_batch=max(64, len(xt), len(fq) * npo), seed=seed, device=self.device)
+        hist = net.fit(torch.as_tensor(xt), T, steps=steps, lr=3e-3)
         xa = features(np.repeat(fn(fq), npo), np.tile(np.arange(npo), len(fq)), npo)
         P = net.forward(torch.as_tensor(xa)).to(torch.float64) * scale    # (nf*np, 2r)
         r = Q.shape[1]
@@ -545,7 +583,7 @@ class FrequencySweep:
 
     def run_warm(self, freqs, n_train: int = 32, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
                  chunk: int | None = None, guess: str = "projection", solver: str = "ilu0", n_anchor: int = 4,
-                 precision: str = "fp32", mlp_steps: int = 1500) -> SweepResult:
+                 precision: str = "fp32", mlp_steps: int = 1500, refine: int = 0) -> SweepResult:
         """Batched sweep: solve n_train evenly spread points, build an initial guess for
         every point from their span (``guess`` = "projection": minimal residual;
         "mlp": the warm-start network; "none": zero), then finish all points with
@@ -560,7 +598,7 @@ class FrequencySweep:
             anchors = self.default_anchors(freqs, n_anchor)
             solve = lambda fr, x0=None: self.run_anchored(fr, anchors=anchors, precision=precision, tol=tol,  # noqa: E731
                                                            restart=min(restart, 60), max_iter=max_iter, x0=x0,
-                                                           chunk=chunk)
+                                                           chunk=chunk, refine=refine)
         else:
             solve = lambda fr, x0=None: self.run(fr, method="batched", tol=tol, restart=restart,  # noqa: E731
                                                  max_iter=max_iter, x0=x0, chunk=chunk)

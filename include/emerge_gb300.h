@@ -134,6 +134,8 @@ int emg_rplan_create(int64_t N, const int64_t* indptr, const int32_t* indices, i
 int64_t emg_rplan_n(const emg_rplan* plan);
 int64_t emg_rplan_nnz(const emg_rplan* plan);
 int64_t emg_rplan_levels(const emg_rplan* plan);
+/* HOST copies of the restricted CSR pattern: indptr (n_solve+1), indices (nnz_r). */
+int emg_rplan_pattern(const emg_rplan* plan, int64_t* indptr_out, int32_t* indices_out);
 void emg_rplan_destroy(emg_rplan* plan);
 
 /* Restricted matrices A_m = E - k2[m] B + sum_p gam[p][m] P_p (m < Bm) from
@@ -179,8 +181,11 @@ int emg_gmres(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_t Bm
 typedef struct emg_slab emg_slab;
 
 /* Slab structure of a restricted plan (host breadth-first search; synchronises
- * ``stream``).  EMG_ERR_LIMIT if a slab is wider than 12288 DOFs. */
-int emg_slab_create(const emg_rplan* plan, void* stream, emg_slab** slab);
+ * ``stream``).  With n_seeds > 0 the search starts from all seeds (HOST int64
+ * restricted indices) at once, e.g. the DOFs next to one end face, which makes
+ * the slabs planar cross-sections; otherwise from a pseudo-peripheral DOF.
+ * EMG_ERR_LIMIT if a slab is wider than 12288 DOFs. */
+int emg_slab_create(const emg_rplan* plan, int64_t n_seeds, const int64_t* seeds, void* stream, emg_slab** slab);
 void emg_slab_destroy(emg_slab* slab);
 /* info[7] (host): slabs, widest slab, dense entries per factor, coupling entries,
  * factors held, precision, perturbed pivots of the last factorization. */
@@ -189,9 +194,12 @@ int emg_slab_info(const emg_slab* slab, int64_t* info);
  * (n_solve): restricted index of each slab position. */
 int emg_slab_levels(const emg_slab* slab, int64_t* off_out, int32_t* perm_out);
 /* Factor the F matrices A[:, amat[f]] (A: [nnz_r][Bm] complex, DEVICE; amat: F
- * HOST int32).  Replaces any factorization held.  Synchronises ``stream``. */
+ * HOST int32).  refine = 1 applies one Newton-Schulz step X <- X (2I - S X) to
+ * every slab inverse (two extra dense products; recovers most of the accuracy
+ * that inverting without pivoting across 64-row tiles loses); 0 = none.
+ * Replaces any factorization held.  Synchronises ``stream``. */
 int emg_slab_factor(emg_slab* slab, int precision, int64_t F, const int32_t* amat, int64_t Bm, const double* A,
-                    void* stream);
+                    int refine, void* stream);
 /* X_out = A_f^-1 X_in column by column, f = cfac[c] (HOST int32, Bc); X_in and
  * X_out are distinct DEVICE [n_solve][Bc] complex arrays. */
 int emg_slab_apply(emg_slab* slab, int64_t Bc, const int32_t* cfac, const double* X_in, double* X_out, void* stream);

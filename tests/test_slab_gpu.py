@@ -89,7 +89,7 @@ def test_fp32_factors_with_fgmres_reach_fp64_accuracy(system):
     X32 = slab.apply(Bt, [0, 0, 1, 1]).cpu().numpy()
     ref = [spla.spsolve(Ks[c // 2].tocsc(), B[:, c]) for c in range(4)]
     e32 = max(np.linalg.norm(X32[:, c] - ref[c]) / np.linalg.norm(ref[c]) for c in range(4))
-    assert e32 < 1e-1
+    assert 1e-8 < e32 < 0.5
     # FGMRES in FP64 around it; column 3 uses the other frequency's factor
     cmat = torch.tensor([0, 0, 1, 1], dtype=torch.int32, device="cuda")
     x, its, res = slab.gmres(vals, Bt, cmat, [0, 0, 1, 0], tol=1e-10, restart=40, max_iter=400)

@@ -75,3 +75,19 @@ def test_warm_start_sweep_agrees_and_saves_iterations(waveguide):
     assert np.all(warm.residuals <= 1e-9)
     assert np.max(np.abs(warm.S - cold.S)) <= 1e-6
     assert warm.iterations.sum() < cold.iterations.sum()
+
+
+def test_mlp_warm_start_saves_iterations_over_cold_start(waveguide):
+    """The trained warm-start network: same S-parameters as the cold anchored sweep,
+    fewer FGMRES iterations on the points it predicts."""
+    from emerge_gb300.solver import FrequencySweep
+    z, field, bcs, eye, asm = waveguide
+    sw = FrequencySweep(asm, field, eye, eye, bcs)
+    freqs = np.linspace(8.5e9, 10.5e9, 17)
+    cold = sw.run_anchored(freqs, n_anchor=1, precision="fp32", tol=1e-10)
+    warm = sw.run_warm(freqs, n_train=5, solver="anchored", n_anchor=1, precision="fp32", guess="mlp", tol=1e-10,
+                       mlp_steps=1500)
+    assert np.all(warm.residuals <= 1e-9)
+    assert np.max(np.abs(warm.S - cold.S)) <= 1e-6
+    assert warm.info["mlp_loss"] < 1e-2
+    assert warm.iterations.sum() < cold.iterations.sum()
