@@ -204,11 +204,14 @@ __global__ void __launch_bounds__(kThreads) k_schur(int64_t wp, int64_t w, int64
 // the inverse also goes to pinv (ld 64).  Grid 1 x 1 x F.
 //
 // Gauss-Jordan on a 64 x 64 shared tile (padded with the identity when tb < 64),
-// two barriers per pivot.  Thread t owns column t/4 and rows t%4 + 4q.  Step c:
-// (S) swap the pivot row p into row c while forming the scaled pivot row and the
-// old column c; (U) rank-1 update, during which the four lanes owning column c+1
-// pick the next pivot (largest |a_rc| below the diagonal, lowest row on ties)
-// with two shuffles.  The row swaps become one column permutation at the end.
+// two barriers per pivot.  Thread t owns column t % 64 and rows t / 64 + 4q, so a
+// warp touches 32 consecutive columns of one row (no bank conflicts).  Step c:
+// every thread reduces the four pivot candidates of column c (one per owner
+// thread, largest |a_rc| below the diagonal, lowest row on ties); (S) the pivot
+// row p is swapped into row c while the scaled pivot row and the old column c are
+// formed; (U) rank-1 update from registers, during which the owners of column
+// c+1 leave their candidates for the next step.  The row swaps become one column
+// permutation at the end.
 template <typename T> __device__ __forceinline__ T crecip(T v) {
     const auto m2 = v.x * v.x + v.y * v.y;
     return mk(v.x / m2, -v.y / m2);
@@ -219,19 +222,21 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
                                                       int64_t totD, int64_t offD, typename C2<R>::T* __restrict__ pinv,
                                                       R rel_thr, int32_t* __restrict__ perturbed) {
     using T = typename C2<R>::T;
+    constexpr int kQ = kTile * kTile / kThreads;   // rows per thread (16)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T(*a)[kTile + 1] = reinterpret_cast<T(*)[kTile + 1]>(smem_raw);
     __shared__ T rowc[kTile], colc[kTile];
     __shared__ int piv[kTile], perm[kTile];
-    __shared__ int s_p;
-    __shared__ T s_pv;
+    __shared__ R cand_m[kThreads / kTile];
+    __shared__ int cand_i[kThreads / kTile];
+    __shared__ T cand_v[kThreads / kTile];
     __shared__ R s_red[kThreads / 32];
     const int64_t f = blockIdx.z;
     T* M = Sinv + f * totD + offD;
     const int64_t k0 = (int64_t)k * kTile;
     const int tb = (int)min((int64_t)kTile, w - k0);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int j = tid >> 2, rq = tid & 3;
+    const int j = tid % kTile, r0 = tid / kTile, slot = r0;
     R mx = 0;
     for (int idx = tid; idx < kTile * kTile; idx += kThreads) {
         const int r = idx / kTile, c = idx % kTile;
@@ -252,48 +257,46 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
 #pragma unroll
     for (int i = 0; i < kThreads / 32; ++i) thr2 = max(thr2, s_red[i]);
     thr2 *= rel_thr * rel_thr;   // |pivot|^2 at or below this is replaced
-    // the four lanes owning column c choose its pivot among rows [c, tb)
-    auto find = [&](int c) {
-        const unsigned mask = 0xFu << (lane & 28);
+    // candidates of column 0 from shared memory
+    if (j == 0) {
         R best = -1;
-        int bi = tb;
+        int bi = kTile;
         T bv = mk((R)0, (R)0);
 #pragma unroll
-        for (int q = 0; q < kTile / 4; ++q) {
-            const int r = rq + 4 * q;
-            if (r >= c && r < tb) {
-                const T v = a[r][c];
+        for (int q = 0; q < kQ; ++q) {
+            const int r = r0 + 4 * q;
+            if (r < tb) {
+                const T v = a[r][0];
                 const R m2 = v.x * v.x + v.y * v.y;
                 if (m2 > best) { best = m2; bi = r; bv = v; }
             }
         }
-#pragma unroll
-        for (int o = 1; o <= 2; o <<= 1) {
-            const R ob = __shfl_xor_sync(mask, best, o);
-            const int oi = __shfl_xor_sync(mask, bi, o);
-            const R ox = __shfl_xor_sync(mask, bv.x, o);
-            const R oy = __shfl_xor_sync(mask, bv.y, o);
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; bv = mk(ox, oy); }
-        }
-        if (rq == 0) {
-            if (!(best > thr2)) {   // also catches a zero column
-                bv = mk(thr2 > 0 ? (R)sqrt(thr2) : (R)1, (R)0);
-                atomicAdd(perturbed + f, 1);
-            }
-            s_p = bi < tb ? bi : c;
-            s_pv = bv;
-            piv[c] = s_p;
-        }
-    };
-    if (j == 0) find(0);
+        cand_m[slot] = best; cand_i[slot] = bi; cand_v[slot] = bv;
+    }
     __syncthreads();
+    T v[kQ];
     for (int c = 0; c < tb; ++c) {
-        const int p = s_p;
-        const T inv = crecip(s_pv);
+        // pivot of column c from the four candidates (same result in every thread)
+        R best = cand_m[0];
+        int p = cand_i[0];
+        T pv = cand_v[0];
+#pragma unroll
+        for (int i = 1; i < kThreads / kTile; ++i) {
+            const R m2 = cand_m[i];
+            const int ii = cand_i[i];
+            if (m2 > best || (m2 == best && ii < p)) { best = m2; p = ii; pv = cand_v[i]; }
+        }
+        if (!(best > thr2)) {   // also catches a zero column
+            pv = mk(thr2 > 0 ? (R)sqrt(thr2) : (R)1, (R)0);
+            if (tid == 0) atomicAdd(perturbed + f, 1);
+        }
+        if (p >= tb) p = c;
+        const T inv = crecip(pv);
         if (tid < kTile) {
             const T vp = a[p][tid];
             if (p != c) a[p][tid] = a[c][tid];
             rowc[tid] = cmul(vp, inv);
+            if (tid == 0) piv[c] = p;
         } else if (tid < 2 * kTile) {
             const int r = tid - kTile;
             colc[r] = r == p ? a[c][c] : a[r][c];
@@ -301,23 +304,38 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
         __syncthreads();
         const T rj = rowc[j];
 #pragma unroll
-        for (int q = 0; q < kTile / 4; ++q) {
-            const int r = rq + 4 * q;
-            T v;
+        for (int q = 0; q < kQ; ++q) v[q] = a[r0 + 4 * q][j];
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) {
+            const int r = r0 + 4 * q;
+            const T cr = colc[r];
             if (r == c) {
-                v = j == c ? inv : rj;
+                v[q] = j == c ? inv : rj;
             } else if (j == c) {
-                const T t = cmul(colc[r], inv);
-                v = mk(-t.x, -t.y);
+                const T t = cmul(cr, inv);
+                v[q] = mk(-t.x, -t.y);
             } else {
-                v = a[r][j];
-                const T t = cmul(colc[r], rj);
-                v.x -= t.x;
-                v.y -= t.y;
+                const T t = cmul(cr, rj);
+                v[q].x -= t.x;
+                v[q].y -= t.y;
             }
-            a[r][j] = v;
         }
-        if (c + 1 < tb && j == c + 1) find(c + 1);
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) a[r0 + 4 * q][j] = v[q];
+        if (j == c + 1) {
+            R bm = -1;
+            int bi = kTile;
+            T bv = mk((R)0, (R)0);
+#pragma unroll
+            for (int q = 0; q < kQ; ++q) {
+                const int r = r0 + 4 * q;
+                if (r > c && r < tb) {
+                    const R m2 = v[q].x * v[q].x + v[q].y * v[q].y;
+                    if (m2 > bm) { bm = m2; bi = r; bv = v[q]; }
+                }
+            }
+            cand_m[slot] = bm; cand_i[slot] = bi; cand_v[slot] = bv;
+        }
         __syncthreads();
     }
     if (tid == 0) {
@@ -331,9 +349,9 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
     T* P = pinv + f * kTile * kTile;
     for (int idx = tid; idx < tb * tb; idx += kThreads) {
         const int r = idx / tb, c = idx % tb;
-        const T v = a[r][perm[c]];
-        M[(k0 + r) * w + k0 + c] = v;
-        P[r * kTile + c] = v;
+        const T x = a[r][perm[c]];
+        M[(k0 + r) * w + k0 + c] = x;
+        P[r * kTile + c] = x;
     }
 }
 

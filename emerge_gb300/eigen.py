@@ -47,6 +47,11 @@ class EigResult:
         return np.sqrt(np.abs(self.eigenvalues.real)) * 299792458.0 / (2 * np.pi)
 
 
+def _sync(device) -> None:
+    if torch.device(device).type == "cuda":
+        torch.cuda.synchronize(device)
+
+
 class ShiftInvertEigen:
     """Eigenpairs of restricted (E, B) value arrays on a RestrictedSystem.
 
@@ -84,30 +89,44 @@ class ShiftInvertEigen:
         return W
 
     def solve(self, nmodes: int, sigma: float, which: str = "LR", block: int = 4, ncv: int | None = None,
-              tol: float = 1e-10, max_restarts: int = 12, precision: str = "fp32", seed: int = 0,
-              inner_tol: float = 1e-12, refine: int = 1) -> EigResult:
-        torch.cuda.synchronize()
+              tol: float = 1e-10, max_restarts: int = 30, precision: str = "fp32", seed: int = 0,
+              inner_tol: float = 1e-12, refine: int = 1, adapt: bool = False) -> EigResult:
+        """nmodes eigenpairs; see the module docstring for ``which``.
+
+        Thick-restarted block Arnoldi: after each Rayleigh-Ritz the wanted Ritz vectors
+        (plus a few extra) are kept, orthonormalised, with Op applied to them taken from
+        the stored products, and the expansion continues from the block not yet
+        expanded.  ``adapt`` (which="LR" only) moves the shift half-way up to a
+        converged lowest Ritz value and re-factors; it is off by default because a shift
+        close to the first mode makes that mode dominate the Krylov space and slows the
+        others."""
+        _sync(self.device)
         t0 = time.perf_counter()
         n = self.sys.n
-        ncv = ncv or max(4 * nmodes, nmodes + 6 * block)
-        ncv = min(ncv, n)
-        A = (self.Er - float(sigma) * self.Br).contiguous()          # E - sigma B (restricted values)
-        self.slab.factor(A, [0], precision, refine)
+        extra = min(4, max(0, n - nmodes))
+        ncv = min(ncv or max(4 * nmodes, 40), n)
         gen = torch.Generator(device="cpu").manual_seed(seed)
         V0 = torch.randn((n, block), generator=gen, dtype=torch.float64).to(self.device).to(torch.complex128)
-        keep = None
         lam = res = X = None
+        sig = float(sigma)
+        factored = None
+        shifts = []
+        V = torch.linalg.qr(V0)[0].contiguous()    # orthonormal basis; Op known for its first j columns
+        OV = []
+        j = 0
         for restart in range(max_restarts + 1):
-            # block Arnoldi basis of Op = (E - sigma B)^-1 B, started from the kept Ritz vectors
-            start = V0 if keep is None else torch.cat([keep, V0], dim=1)
-            Q, _ = torch.linalg.qr(start)
-            V = Q.contiguous()
-            OV = []
-            j = 0
-            while V.shape[1] < ncv:
-                Vj = V[:, j:j + block] if j + block <= V.shape[1] else V[:, j:]
-                if Vj.shape[1] == 0:
-                    break
+            if factored != sig:
+                A = (self.Er - sig * self.Br).contiguous()              # E - sigma B (restricted values)
+                self.slab.factor(A, [0], precision, refine)
+                factored = sig
+                shifts.append(sig)
+                if restart > 0:      # a new shift invalidates Op V: restart from the Ritz vectors
+                    V = torch.linalg.qr(X)[0].contiguous()
+                    OV = []
+                    j = 0
+            # block Arnoldi on Op = (E - sigma B)^-1 B up to ncv columns
+            while j < ncv and j < V.shape[1]:
+                Vj = V[:, j:j + block]
                 W = self._op(A, Vj.contiguous(), inner_tol)
                 OV.append(W)
                 j += Vj.shape[1]
@@ -115,28 +134,46 @@ class ShiftInvertEigen:
                 Qw, Rw = torch.linalg.qr(W)
                 good = torch.abs(torch.diagonal(Rw)) > 1e-10 * torch.linalg.norm(W, dim=0).max().clamp_min(1e-300)
                 V = torch.cat([V, Qw[:, good]], dim=1).contiguous()
-            # Op applied to every basis vector used; Rayleigh-Ritz on span(V[:, :j])
+            # Rayleigh-Ritz on span(V[:, :j])
             Vb = V[:, :j]
             OVm = torch.cat(OV, dim=1)[:, :j]
-            H = Vb.conj().T @ OVm                                       # (j, j) FP64
+            H = Vb.conj().T @ OVm                                        # (j, j) FP64
             theta, Y = torch.linalg.eig(H)
             th = theta.cpu().numpy()
             order = np.argsort(-np.abs(th)) if which == "LM" else np.argsort(-th.real)
-            sel = order[:nmodes]
-            Ysel = Y[:, torch.as_tensor(sel, device=self.device)]
-            X = Vb @ Ysel
-            X = X / torch.linalg.norm(X, dim=0, keepdim=True)
-            lam = sigma + 1.0 / th[sel]
-            lam, res, X = self._refine(X, lam)
-            if np.all(res <= tol):
+            sel = torch.as_tensor(order[: nmodes + extra], device=self.device)
+            Yk = Y[:, sel]
+            X = Vb @ Yk
+            nrm = torch.linalg.norm(X, dim=0, keepdim=True)
+            X = X / nrm
+            lam, res, X = self._refine(X, sig + 1.0 / th[order[: nmodes + extra]])
+            if np.all(res[:nmodes] <= tol):
                 break
-            keep = X
-        torch.cuda.synchronize()
+            # thick restart: orthonormalised Ritz vectors (Op on them from the stored
+            # products, no new solves) followed by the block not yet expanded
+            Qk, Rk = torch.linalg.qr(X)
+            OVk = torch.linalg.solve_triangular(Rk.T, ((OVm @ Yk) / nrm).T, upper=False).T
+            nxt = V[:, j:]
+            if nxt.shape[1] == 0:      # the last block was rank deficient: continue from a new random block
+                nxt = torch.randn((n, block), generator=gen, dtype=torch.float64).to(self.device).to(torch.complex128)
+            nxt = torch.linalg.qr(self._orth(Qk, nxt))[0]
+            V = torch.cat([Qk, nxt], dim=1).contiguous()
+            OV = [OVk.contiguous()]
+            j = Qk.shape[1]
+            if adapt and which == "LR":
+                lo = int(np.argmin(lam.real))
+                l1 = float(lam.real[lo])
+                if l1 > sig and res[lo] < 1e-6:
+                    nxt_sig = sig + 0.5 * (l1 - sig)
+                    if nxt_sig > sig * 1.5:
+                        sig = nxt_sig
+        _sync(self.device)
         secs = time.perf_counter() - t0
         info = {"restarts": restart, "basis": int(j), "solves": self.solves, "inner_iterations": self.inner_iterations,
-                **self.slab.info()}
+                "shifts": shifts, **self.slab.info()}
+        lam, res, X = lam[:nmodes], res[:nmodes], X[:, :nmodes]
         o = np.argsort(lam.real)
-        return EigResult(lam[o], X[:, torch.as_tensor(o, device=self.device)], res[o], float(sigma), secs, info)
+        return EigResult(lam[o], X[:, torch.as_tensor(o, device=self.device)], res[o], float(sig), secs, info)
 
     def _refine(self, X, lam):
         """FP64 Rayleigh quotients x^H E x / x^H B x and residuals of unit vectors X."""
