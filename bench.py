@@ -401,6 +401,7 @@ def main():
     ap.add_argument("--sweep-ilu-iters", type=int, default=1000)
     ap.add_argument("--sweep-cpu", type=int, default=1, help="points solved by SciPy SuperLU on the host")
     ap.add_argument("--sweep-tol", type=float, default=1e-8)
+    ap.add_argument("--sweep-only", action="store_true", help="print only the sweep measurement")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -413,6 +414,9 @@ def main():
         dist.init_process_group(backend)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.sweep_only:
+        if rank == 0:
+            print(json.dumps(run_sweep(args)))
     else:
         run_gpu(args, rank, world)
     if world > 1:

@@ -49,6 +49,11 @@ SIGNATURES = {
     "emg_gmres": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int,
                                  ctypes.c_double, c_vp, c_vp, c_vp]),
     "emg_rplan_pattern": (ctypes.c_int, [c_vp, c_vp, c_vp]),
+    "emg_spmv_family": (ctypes.c_int, [c_vp, c_i64, ctypes.c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "emg_gmres_slab_family": (ctypes.c_int, [c_vp, c_vp, c_i64, ctypes.c_int, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_double, c_vp, c_vp, c_vp]),
+    "emg_gmres_slab_mixed": (ctypes.c_int, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_double, ctypes.c_double, c_vp, c_vp, c_vp, c_vp]),
     "emg_slab_create": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, ctypes.POINTER(c_vp)]),
     "emg_slab_destroy": (None, [c_vp]),
     "emg_slab_info": (ctypes.c_int, [c_vp, c_vp]),

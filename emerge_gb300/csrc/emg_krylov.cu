@@ -205,6 +205,30 @@ __global__ void k_spmv(int64_t n, int64_t Bc, const int32_t* __restrict__ cmat, 
     }
 }
 
+// Y = A_c X with A_c = sum_a coef[c][a] fam[a] formed on the fly (thread per (row,
+// column); the family values of a row are shared by the warp's columns).
+__global__ void k_spmv_fam(int64_t n, int64_t nnz, int64_t Bc, int nfam, const double2* __restrict__ fam,
+                           const double2* __restrict__ coef, const int64_t* __restrict__ rptr,
+                           const int32_t* __restrict__ rind, const double2* __restrict__ X,
+                           const double2* __restrict__ Bv, double2* __restrict__ Y) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / Bc, c = t % Bc;
+        double2 cf[kMaxFamily];
+#pragma unroll
+        for (int a = 0; a < kMaxFamily; ++a) cf[a] = a < nfam ? coef[c * nfam + a] : make_double2(0.0, 0.0);
+        double2 s = make_double2(0.0, 0.0);
+        for (int64_t k = rptr[i]; k < rptr[i + 1]; ++k) {
+            double2 v = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int a = 0; a < kMaxFamily; ++a)
+                if (a < nfam) v = cadd(v, cmul(cf[a], fam[a * nnz + k]));
+            s = cadd(s, cmul(v, X[(int64_t)rind[k] * Bc + c]));
+        }
+        Y[t] = Bv ? csub(Bv[t], s) : s;
+    }
+}
+
 // Column-wise partial dots: part[blk][j][c] = sum_{rows in blk} conj(V_j[r,c]) W[r,c], j < nj.
 constexpr int kDotRows = 1024;
 constexpr int kMaxRestart = 256;
@@ -396,6 +420,158 @@ __global__ void k_real(int64_t Bc, const double2* __restrict__ in, double* __res
 __global__ void k_sqrt_real(int64_t Bc, const double2* __restrict__ in, double* __restrict__ out) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c < Bc) out[c] = sqrt(fmax(in[c].x, 0.0));
+}
+
+// ---- FP32-vector kernels for the inner solves of the mixed-precision refinement ----
+__device__ __forceinline__ float2 fmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }
+__device__ __forceinline__ void ffma(float2& acc, float2 a, float2 b) {
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(-a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(a.y, b.x, acc.y);
+}
+
+__global__ void k_spmv32(int64_t n, int64_t Bc, const int32_t* __restrict__ cmat, int64_t Bm,
+                         const int64_t* __restrict__ rptr, const int32_t* __restrict__ rind, const float2* __restrict__ A,
+                         const float2* __restrict__ X, const float2* __restrict__ Bv, float2* __restrict__ Y) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / Bc, c = t % Bc;
+        const int64_t m = cmat[c];
+        float2 s = make_float2(0.f, 0.f);
+        for (int64_t k = rptr[i]; k < rptr[i + 1]; ++k) ffma(s, A[k * Bm + m], X[(int64_t)rind[k] * Bc + c]);
+        Y[t] = Bv ? make_float2(Bv[t].x - s.x, Bv[t].y - s.y) : s;
+    }
+}
+
+__global__ void k_spmv32_w(int64_t n, int64_t Bc, const int32_t* __restrict__ cmat, int64_t Bm,
+                           const int64_t* __restrict__ rptr, const int32_t* __restrict__ rind, const float2* __restrict__ A,
+                           const float2* __restrict__ X, const float2* __restrict__ Bv, float2* __restrict__ Y) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    float2 acc[kSmallBc];
+#pragma unroll
+    for (int c = 0; c < kSmallBc; ++c) acc[c] = make_float2(0.f, 0.f);
+    for (int64_t k = rptr[i] + lane; k < rptr[i + 1]; k += 32) {
+        const int64_t col = rind[k];
+#pragma unroll
+        for (int c = 0; c < kSmallBc; ++c)
+            if (c < Bc) ffma(acc[c], A[k * Bm + cmat[c]], X[col * Bc + c]);
+    }
+#pragma unroll
+    for (int c = 0; c < kSmallBc; ++c) {
+        if (c >= Bc) break;
+        float2 v = acc[c];
+        for (int o = 16; o > 0; o >>= 1) {
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (lane == 0) Y[i * Bc + c] = Bv ? make_float2(Bv[i * Bc + c].x - v.x, Bv[i * Bc + c].y - v.y) : v;
+    }
+}
+
+// partial dots over kDotRows rows: FP32 products and running sums, FP64 block partials
+__global__ void k_dots32(int64_t n, int64_t Bc, int nj, const float2* __restrict__ V, int64_t vstride,
+                         const float2* __restrict__ W, double2* __restrict__ part) {
+    const int64_t c = blockIdx.y * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= Bc) return;
+    const int64_t r0 = (int64_t)blockIdx.x * kDotRows, r1 = min(n, r0 + kDotRows);
+    for (int j = 0; j < nj; ++j) {
+        float2 s = make_float2(0.f, 0.f);
+        const float2* Vj = V + j * vstride;
+        for (int64_t r = r0; r < r1; ++r) {
+            const float2 p = fmulc(Vj[r * Bc + c], W[r * Bc + c]);
+            s.x += p.x;
+            s.y += p.y;
+        }
+        part[((int64_t)blockIdx.x * nj + j) * Bc + c] = make_double2(s.x, s.y);
+    }
+}
+
+__global__ void k_dots32_small(int64_t n, int64_t Bc, int nj, const float2* __restrict__ V, int64_t vstride,
+                               const float2* __restrict__ W, double2* __restrict__ part) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int64_t r0 = (int64_t)blockIdx.x * kDotRows, r1 = min(n, r0 + kDotRows);
+    for (int64_t pr = warp; pr < (int64_t)nj * Bc; pr += nw) {
+        const int64_t j = pr / Bc, c = pr % Bc;
+        const float2* Vj = V + j * vstride;
+        float2 s = make_float2(0.f, 0.f);
+        for (int64_t r = r0 + lane; r < r1; r += 32) {
+            const float2 p = fmulc(Vj[r * Bc + c], W[r * Bc + c]);
+            s.x += p.x;
+            s.y += p.y;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+            s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+        }
+        if (lane == 0) part[((int64_t)blockIdx.x * nj + j) * Bc + c] = make_double2(s.x, s.y);
+    }
+}
+
+__global__ void k_orth32(int64_t n, int64_t Bc, int nj, const float2* __restrict__ V, int64_t vstride,
+                         const double2* __restrict__ h, const int32_t* __restrict__ active, float2* __restrict__ W) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = t % Bc;
+        if (!active[c]) continue;
+        float2 w = W[t];
+        for (int j = 0; j < nj; ++j) {
+            const double2 hj = h[(int64_t)j * Bc + c];
+            ffma(w, make_float2(-(float)hj.x, -(float)hj.y), V[j * vstride + t]);
+        }
+        W[t] = w;
+    }
+}
+
+__global__ void k_scale32(int64_t n, int64_t Bc, const double* __restrict__ scale, const float2* __restrict__ W,
+                          float2* __restrict__ Vout) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const float sc = (float)scale[t % Bc];
+        const float2 w = W[t];
+        Vout[t] = make_float2(w.x * sc, w.y * sc);
+    }
+}
+
+__global__ void k_combine32(int64_t n, int64_t Bc, int nj, const float2* __restrict__ Z, int64_t zstride,
+                            const double2* __restrict__ y, float2* __restrict__ X) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = t % Bc;
+        float2 x = X[t];
+        for (int j = 0; j < nj; ++j) {
+            const double2 yj = y[(int64_t)j * Bc + c];
+            ffma(x, make_float2((float)yj.x, (float)yj.y), Z[j * zstride + t]);
+        }
+        X[t] = x;
+    }
+}
+
+// out = r * scale[c] in FP32; x += scale[c] * d in FP64; FP64 -> FP32 copy of matrix values
+__global__ void k_to32_scaled(int64_t n, int64_t Bc, const double2* __restrict__ r, const double* __restrict__ scale,
+                              float2* __restrict__ out) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const double sc = scale[t % Bc];
+        out[t] = make_float2((float)(r[t].x * sc), (float)(r[t].y * sc));
+    }
+}
+
+__global__ void k_axpy_from32(int64_t n, int64_t Bc, const float2* __restrict__ d, const double* __restrict__ scale,
+                              double2* __restrict__ x) {
+    const int64_t total = n * Bc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const double sc = scale[t % Bc];
+        x[t].x += sc * (double)d[t].x;
+        x[t].y += sc * (double)d[t].y;
+    }
+}
+
+__global__ void k_to32(int64_t nv, const double2* __restrict__ in, float2* __restrict__ out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nv; t += (int64_t)gridDim.x * blockDim.x)
+        out[t] = make_float2((float)in[t].x, (float)in[t].y);
 }
 
 }  // namespace kry
@@ -617,6 +793,22 @@ extern "C" int emg_spmv(const emg_rplan* p, int64_t Bc, const int32_t* cmat, int
     return EMG_OK;
 }
 
+extern "C" int emg_spmv_family(const emg_rplan* p, int64_t Bc, int nfam, const double* fam, const double* coef,
+                               const double* X, const double* Bv, double* Y, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p && fam && coef && X && Y && Bc > 0 && nfam >= 1 && nfam <= kMaxFamily,
+                  "emg_spmv_family: bad argument");
+    if (p->ns == 0) return EMG_OK;
+    MatArg A;
+    A.nfam = nfam;
+    A.fam = reinterpret_cast<const double2*>(fam);
+    A.coef = reinterpret_cast<const double2*>(coef);
+    spmv_op(p, Bc, A, reinterpret_cast<const double2*>(X), reinterpret_cast<const double2*>(Bv),
+            reinterpret_cast<double2*>(Y), (cudaStream_t)stream);
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+
 extern "C" int emg_rplan_gather(const emg_rplan* p, int64_t Bc, const double* full, double* out, void* stream) {
     using namespace emg;
     EMG_CHECK_ARG(p && full && out && Bc > 0, "emg_rplan_gather: bad argument");
@@ -667,9 +859,19 @@ void dots(int64_t n, int64_t Bc, int nj, const double2* V, int64_t vstride, cons
 }  // namespace
 
 namespace emg {
-int gmres_run(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double2* A, const double2* rhs,
-              double2* x, int restart, int max_iter, double tol, int32_t* iters_out, double* resid_out,
-              cudaStream_t caller, Precond& M, bool flexible) {
+void spmv_op(const emg_rplan* p, int64_t Bc, const MatArg& A, const double2* X, const double2* Bv, double2* Y,
+             cudaStream_t s) {
+    if (A.nfam > 0)
+        kry::k_spmv_fam<<<grid_for(p->ns * Bc, 256), 256, 0, s>>>(p->ns, p->nnz, Bc, A.nfam, A.fam, A.coef, p->rptr,
+                                                                  p->rind, X, Bv, Y);
+    else
+        spmv(p, Bc, A.cmat, A.Bm, A.A, X, Bv, Y, s);
+}
+}  // namespace emg
+
+namespace emg {
+int gmres_run(emg_rplan* p, int64_t Bc, const MatArg& A, const double2* rhs, double2* x, int restart, int max_iter,
+              double tol, int32_t* iters_out, double* resid_out, cudaStream_t caller, Precond& M, bool flexible) {
     const int64_t n = p->ns;
     if (n == 0) return EMG_OK;
     {
@@ -747,7 +949,7 @@ int gmres_run(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const d
         double2* Mv = flexible ? Z + (int64_t)j * vec : Tv;
         int rc = M.apply(Vj, Mv, s);
         if (rc) return rc;
-        spmv(p, Bc, cmat, Bm, A, Mv, nullptr, W, s);
+        spmv_op(p, Bc, A, Mv, nullptr, W, s);
         // CGS2: two passes of h = V^H w, w -= V h
         const unsigned hgrid = (unsigned)(((int64_t)(j + 1) * Bc + 127) / 128);
         dots(n, Bc, j + 1, V, vec, W, part, nblk, s);
@@ -773,7 +975,7 @@ int gmres_run(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const d
     std::vector<int32_t> hact(Bc), hprev(Bc), hits(Bc, 0);
     while (total < max_iter) {
         // r = b - A x ; V0 = r / ||r||
-        spmv(p, Bc, cmat, Bm, A, x, rhs, W, s);
+        spmv_op(p, Bc, A, x, rhs, W, s);
         double2* rr = norms2(W);
         kry::k_restart_cols<<<cgrid, 128, 0, s>>>(Bc, rr, bn, tol, g, vs, act, len, res, m + 1);
         kry::k_scale_cols<<<grid_for(vec, T), T, 0, s>>>(n, Bc, vs, W, V);
@@ -825,7 +1027,7 @@ int gmres_run(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const d
         EMG_CUDA(cudaGetLastError());
     }
     // explicit final residual
-    spmv(p, Bc, cmat, Bm, A, x, rhs, W, s);
+    spmv_op(p, Bc, A, x, rhs, W, s);
     double2* rr = norms2(W);
     std::vector<double2> hr(Bc);
     std::vector<double> hb(Bc), hres(Bc);
@@ -836,6 +1038,245 @@ int gmres_run(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const d
     EMG_CUDA(cudaMemcpyAsync(resid_out, hres.data(), sizeof(double) * Bc, cudaMemcpyHostToDevice, s));
     EMG_CUDA(cudaMemcpyAsync(iters_out, hits.data(), sizeof(int32_t) * Bc, cudaMemcpyHostToDevice, s));
     EMG_CUDA(cudaStreamSynchronize(s));
+    EMG_CUDA(cudaEventRecord(p->ev_out, s));
+    EMG_CUDA(cudaStreamWaitEvent(caller, p->ev_out, 0));
+    return EMG_OK;
+}
+}  // namespace emg
+
+namespace emg {
+namespace {
+void spmv32(const emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const float2* A, const float2* X,
+            const float2* Bv, float2* Y, cudaStream_t s) {
+    const int64_t n = p->ns;
+    if (Bc <= kry::kSmallBc)
+        kry::k_spmv32_w<<<(unsigned)((n * 32 + 127) / 128), 128, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, X, Bv,
+                                                                           Y);
+    else
+        kry::k_spmv32<<<grid_for(n * Bc, 256), 256, 0, s>>>(n, Bc, cmat, Bm, p->rptr, p->rind, A, X, Bv, Y);
+}
+
+void dots32(int64_t n, int64_t Bc, int nj, const float2* V, int64_t vstride, const float2* W, double2* part,
+            int64_t nblk, cudaStream_t s) {
+    if (Bc < 32) {
+        kry::k_dots32_small<<<(unsigned)nblk, 256, 0, s>>>(n, Bc, nj, V, vstride, W, part);
+    } else {
+        const dim3 g((unsigned)nblk, (unsigned)((Bc + 127) / 128));
+        kry::k_dots32<<<g, 128, 0, s>>>(n, Bc, nj, V, vstride, W, part);
+    }
+}
+
+// Workspace of the inner FP32 FGMRES (carved once per ir_run, reused by every step
+// so the captured Arnoldi-step graphs stay valid across refinement steps).
+struct Inner32 {
+    int m = 0;
+    int64_t vec = 0, nblk = 0;
+    float2 *V = nullptr, *Z = nullptr, *W = nullptr;
+    double2 *part = nullptr, *h1 = nullptr, *h2 = nullptr, *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr,
+            *y = nullptr;
+    double *bn = nullptr, *vs = nullptr, *wn = nullptr, *res = nullptr;
+    int32_t *act = nullptr, *len = nullptr;
+    std::vector<cudaGraphExec_t> graphs;
+    ~Inner32() {
+        for (auto& e : graphs)
+            if (e) cudaGraphExecDestroy(e);
+    }
+};
+
+// FGMRES(m) on FP32 vectors from x = 0; hits[c] = iterations of column c.
+int gmres32(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const float2* A32, const float2* rhs,
+            float2* x, int max_iter, double tol, Inner32& w, std::vector<int32_t>& hits, cudaStream_t s,
+            Precond32& M) {
+    const int64_t n = p->ns, vec = w.vec, nblk = w.nblk;
+    const int m = w.m, T = 256;
+    const unsigned cgrid = (unsigned)((Bc + 127) / 128);
+    auto norms2 = [&](const float2* Vv) {
+        dots32(n, Bc, 1, Vv, vec, Vv, w.part, nblk, s);
+        kry::k_dots_final<<<cgrid, 128, 0, s>>>(nblk, Bc, 1, w.part, w.h1);
+        return w.h1;
+    };
+    kry::k_sqrt_real<<<cgrid, 128, 0, s>>>(Bc, norms2(rhs), w.bn);
+    auto step = [&](int j) -> int {
+        float2* Vj = w.V + (int64_t)j * vec;
+        float2* Zj = w.Z + (int64_t)j * vec;
+        int rc = M.apply(Vj, Zj, s);
+        if (rc) return rc;
+        spmv32(p, Bc, cmat, Bm, A32, Zj, nullptr, w.W, s);
+        const unsigned hgrid = (unsigned)(((int64_t)(j + 1) * Bc + 127) / 128);
+        dots32(n, Bc, j + 1, w.V, vec, w.W, w.part, nblk, s);
+        kry::k_dots_final<<<hgrid, 128, 0, s>>>(nblk, Bc, j + 1, w.part, w.h1);
+        kry::k_orth32<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j + 1, w.V, vec, w.h1, w.act, w.W);
+        dots32(n, Bc, j + 1, w.V, vec, w.W, w.part, nblk, s);
+        kry::k_dots_final<<<hgrid, 128, 0, s>>>(nblk, Bc, j + 1, w.part, w.h2);
+        kry::k_orth32<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j + 1, w.V, vec, w.h2, w.act, w.W);
+        dots32(n, Bc, 1, w.W, vec, w.W, w.part, nblk, s);
+        kry::k_dots_final<<<cgrid, 128, 0, s>>>(nblk, Bc, 1, w.part, w.y);
+        kry::k_real<<<cgrid, 128, 0, s>>>(Bc, w.y, w.wn);
+        kry::k_arnoldi_col<<<cgrid, 128, 0, s>>>(Bc, j, m, w.h1, w.h2, w.wn, w.H, w.cs, w.sn, w.g, w.bn, tol, w.act,
+                                                 w.len, w.vs, w.res);
+        kry::k_scale32<<<grid_for(vec, T), T, 0, s>>>(n, Bc, w.vs, w.W, w.V + (int64_t)(j + 1) * vec);
+        EMG_CUDA(cudaGetLastError());
+        return EMG_OK;
+    };
+    hits.assign(Bc, 0);
+    std::vector<int32_t> hact(Bc), hprev(Bc);
+    int total = 0;
+    while (total < max_iter) {
+        spmv32(p, Bc, cmat, Bm, A32, x, rhs, w.W, s);   // W = rhs - A32 x
+        double2* rr = norms2(w.W);
+        kry::k_restart_cols<<<cgrid, 128, 0, s>>>(Bc, rr, w.bn, tol, w.g, w.vs, w.act, w.len, w.res, m + 1);
+        kry::k_scale32<<<grid_for(vec, T), T, 0, s>>>(n, Bc, w.vs, w.W, w.V);
+        EMG_CUDA(cudaGetLastError());
+        EMG_CUDA(cudaMemcpyAsync(hact.data(), w.act, sizeof(int32_t) * Bc, cudaMemcpyDeviceToHost, s));
+        EMG_CUDA(cudaStreamSynchronize(s));
+        bool any = false;
+        for (int64_t c = 0; c < Bc; ++c) any |= hact[c] != 0;
+        if (!any) break;
+        int j = 0;
+        while (j < m && total < max_iter) {
+            if (!w.graphs[j]) {
+                cudaGraph_t gr = nullptr;
+                EMG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                const int rc = step(j);
+                const cudaError_t ec = cudaStreamEndCapture(s, &gr);
+                if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+                if (ec != cudaSuccess) return cuda_status(ec, "cudaStreamEndCapture");
+                const cudaError_t ei = cudaGraphInstantiate(&w.graphs[j], gr, 0);
+                cudaGraphDestroy(gr);
+                if (ei != cudaSuccess) return cuda_status(ei, "cudaGraphInstantiate");
+            }
+            hprev = hact;
+            EMG_CUDA(cudaGraphLaunch(w.graphs[j], s));
+            ++j;
+            ++total;
+            EMG_CUDA(cudaMemcpyAsync(hact.data(), w.act, sizeof(int32_t) * Bc, cudaMemcpyDeviceToHost, s));
+            EMG_CUDA(cudaStreamSynchronize(s));
+            bool any2 = false;
+            for (int64_t c = 0; c < Bc; ++c) {
+                if (hprev[c]) hits[c] = total;
+                any2 |= hact[c] != 0;
+            }
+            if (!any2) break;
+        }
+        kry::k_backsolve<<<cgrid, 128, 0, s>>>(Bc, m, w.H, w.g, w.len, w.y, j);
+        kry::k_combine32<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j, w.Z, vec, w.y, x);
+        EMG_CUDA(cudaGetLastError());
+    }
+    return EMG_OK;
+}
+}  // namespace
+
+int ir_run(emg_rplan* p, int64_t Bc, const MatArg& A, const float2* A32, const double2* rhs, double2* x, int restart,
+           int max_iter, double tol, double inner_tol, int32_t* iters_out, double* resid_out, int32_t* steps_out,
+           cudaStream_t caller, Precond32& M) {
+    const int64_t n = p->ns;
+    if (n == 0) return EMG_OK;
+    {
+        const int rc = M.prepare(Bc);
+        if (rc) return rc;
+    }
+    EMG_CUDA(cudaEventRecord(p->ev_in, caller));
+    EMG_CUDA(cudaStreamWaitEvent(p->gs, p->ev_in, 0));
+    cudaStream_t s = p->gs;
+    const int m = restart, T = 256;
+    const int64_t vec = n * Bc, nblk = (n + kry::kDotRows - 1) / kry::kDotRows;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
+    const size_t oR64 = take(sizeof(double2) * vec), oR32 = take(sizeof(float2) * vec), oD32 = take(sizeof(float2) * vec);
+    const size_t oV = take(sizeof(float2) * vec * (m + 1)), oZ = take(sizeof(float2) * vec * m);
+    const size_t oW = take(sizeof(float2) * vec);
+    const size_t oPart = take(sizeof(double2) * nblk * (m + 1) * Bc);
+    const size_t oH1 = take(sizeof(double2) * (m + 1) * Bc), oH2 = take(sizeof(double2) * (m + 1) * Bc);
+    const size_t oH = take(sizeof(double2) * m * m * Bc), oCs = take(sizeof(double2) * m * Bc);
+    const size_t oSn = take(sizeof(double2) * m * Bc), oG = take(sizeof(double2) * (m + 1) * Bc);
+    const size_t oY = take(sizeof(double2) * (m + 1) * Bc);
+    const size_t oBn = take(sizeof(double) * Bc), oVs = take(sizeof(double) * Bc), oWn = take(sizeof(double) * Bc);
+    const size_t oRes = take(sizeof(double) * Bc), oAct = take(sizeof(int32_t) * Bc), oLen = take(sizeof(int32_t) * Bc);
+    const size_t oBn64 = take(sizeof(double) * Bc), oRn = take(sizeof(double) * Bc), oSc = take(sizeof(double) * Bc);
+    if (off > p->ws_bytes) {
+        if (p->ws) cudaFree(p->ws);
+        p->ws = nullptr;
+        p->ws_bytes = 0;
+        EMG_CUDA(cudaMalloc(&p->ws, off));
+        p->ws_bytes = off;
+    }
+    char* base = static_cast<char*>(p->ws);
+    auto* r64 = reinterpret_cast<double2*>(base + oR64);
+    auto* r32 = reinterpret_cast<float2*>(base + oR32);
+    auto* d32 = reinterpret_cast<float2*>(base + oD32);
+    Inner32 w;
+    w.m = m;
+    w.vec = vec;
+    w.nblk = nblk;
+    w.V = reinterpret_cast<float2*>(base + oV);
+    w.Z = reinterpret_cast<float2*>(base + oZ);
+    w.W = reinterpret_cast<float2*>(base + oW);
+    w.part = reinterpret_cast<double2*>(base + oPart);
+    w.h1 = reinterpret_cast<double2*>(base + oH1);
+    w.h2 = reinterpret_cast<double2*>(base + oH2);
+    w.H = reinterpret_cast<double2*>(base + oH);
+    w.cs = reinterpret_cast<double2*>(base + oCs);
+    w.sn = reinterpret_cast<double2*>(base + oSn);
+    w.g = reinterpret_cast<double2*>(base + oG);
+    w.y = reinterpret_cast<double2*>(base + oY);
+    w.bn = reinterpret_cast<double*>(base + oBn);
+    w.vs = reinterpret_cast<double*>(base + oVs);
+    w.wn = reinterpret_cast<double*>(base + oWn);
+    w.res = reinterpret_cast<double*>(base + oRes);
+    w.act = reinterpret_cast<int32_t*>(base + oAct);
+    w.len = reinterpret_cast<int32_t*>(base + oLen);
+    w.graphs.assign(m, nullptr);
+    auto* bn64 = reinterpret_cast<double*>(base + oBn64);
+    auto* rn = reinterpret_cast<double*>(base + oRn);
+    auto* sc = reinterpret_cast<double*>(base + oSc);
+    const unsigned cgrid = (unsigned)((Bc + 127) / 128);
+    // ||b|| in FP64
+    dots(n, Bc, 1, rhs, vec, rhs, w.part, nblk, s);
+    kry::k_dots_final<<<cgrid, 128, 0, s>>>(nblk, Bc, 1, w.part, w.h1);
+    kry::k_sqrt_real<<<cgrid, 128, 0, s>>>(Bc, w.h1, bn64);
+    std::vector<double> hb(Bc), hr(Bc), hs(Bc), rel(Bc);
+    EMG_CUDA(cudaMemcpyAsync(hb.data(), bn64, sizeof(double) * Bc, cudaMemcpyDeviceToHost, s));
+    std::vector<int32_t> tot(Bc, 0), hits;
+    int steps = 0, used = 0;
+    constexpr int kMaxSteps = 12;
+    for (;;) {
+        // true residual in FP64
+        spmv_op(p, Bc, A, x, rhs, r64, s);
+        dots(n, Bc, 1, r64, vec, r64, w.part, nblk, s);
+        kry::k_dots_final<<<cgrid, 128, 0, s>>>(nblk, Bc, 1, w.part, w.h1);
+        kry::k_sqrt_real<<<cgrid, 128, 0, s>>>(Bc, w.h1, rn);
+        EMG_CUDA(cudaGetLastError());
+        EMG_CUDA(cudaMemcpyAsync(hr.data(), rn, sizeof(double) * Bc, cudaMemcpyDeviceToHost, s));
+        EMG_CUDA(cudaStreamSynchronize(s));
+        bool all = true;
+        for (int64_t c = 0; c < Bc; ++c) {
+            rel[c] = hb[c] > 0 ? hr[c] / hb[c] : 0.0;
+            all &= rel[c] <= tol;
+        }
+        if (all || steps >= kMaxSteps || used >= max_iter) break;
+        // inner solve of A d = r / ||r|| for the unconverged columns
+        for (int64_t c = 0; c < Bc; ++c) hs[c] = rel[c] > tol ? 1.0 / hr[c] : 0.0;
+        EMG_CUDA(cudaMemcpyAsync(sc, hs.data(), sizeof(double) * Bc, cudaMemcpyHostToDevice, s));
+        kry::k_to32_scaled<<<grid_for(vec, T), T, 0, s>>>(n, Bc, r64, sc, r32);
+        EMG_CUDA(cudaMemsetAsync(d32, 0, sizeof(float2) * vec, s));
+        const int rc = gmres32(p, Bc, A.cmat, A.Bm, A32, r32, d32, max_iter - used, inner_tol, w, hits, s, M);
+        if (rc) return rc;
+        int mx = 0;
+        for (int64_t c = 0; c < Bc; ++c) {
+            tot[c] += hits[c];
+            mx = std::max(mx, (int)hits[c]);
+            hs[c] = rel[c] > tol ? hr[c] : 0.0;
+        }
+        used += std::max(mx, 1);
+        EMG_CUDA(cudaMemcpyAsync(sc, hs.data(), sizeof(double) * Bc, cudaMemcpyHostToDevice, s));
+        kry::k_axpy_from32<<<grid_for(vec, T), T, 0, s>>>(n, Bc, d32, sc, x);
+        EMG_CUDA(cudaGetLastError());
+        ++steps;
+    }
+    EMG_CUDA(cudaMemcpyAsync(resid_out, rel.data(), sizeof(double) * Bc, cudaMemcpyHostToDevice, s));
+    EMG_CUDA(cudaMemcpyAsync(iters_out, tot.data(), sizeof(int32_t) * Bc, cudaMemcpyHostToDevice, s));
+    EMG_CUDA(cudaStreamSynchronize(s));
+    if (steps_out) *steps_out = steps;
     EMG_CUDA(cudaEventRecord(p->ev_out, s));
     EMG_CUDA(cudaStreamWaitEvent(caller, p->ev_out, 0));
     return EMG_OK;
@@ -868,7 +1309,10 @@ extern "C" int emg_gmres(const emg_rplan* pc, int64_t Bc, const int32_t* cmat, i
     EMG_CHECK_ARG(restart >= 1 && restart <= kry::kMaxRestart && max_iter >= 1 && tol > 0,
                   "emg_gmres: restart must be in [1, 256]");
     IluPrecond M(p, Bc, cmat, Bm, reinterpret_cast<const double2*>(LU_));
-    return gmres_run(p, Bc, cmat, Bm, reinterpret_cast<const double2*>(A_), reinterpret_cast<const double2*>(rhs_),
-                     reinterpret_cast<double2*>(x_), restart, max_iter, tol, iters_out, resid_out, (cudaStream_t)stream,
-                     M, false);
+    MatArg A;
+    A.A = reinterpret_cast<const double2*>(A_);
+    A.Bm = Bm;
+    A.cmat = cmat;
+    return gmres_run(p, Bc, A, reinterpret_cast<const double2*>(rhs_), reinterpret_cast<double2*>(x_), restart,
+                     max_iter, tol, iters_out, resid_out, (cudaStream_t)stream, M, false);
 }

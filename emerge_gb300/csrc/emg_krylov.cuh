@@ -39,12 +39,44 @@ struct Precond {
     virtual int apply(const double2* in, double2* out, cudaStream_t s) = 0;   // in and out do not alias
 };
 
-// Restarted GMRES(restart) with CGS2 over Bc lockstep columns (column c uses
-// matrix cmat[c] of Bm).  flexible: keep z_j = M^-1 v_j and update x with them
-// (FGMRES, required when M^-1 is not an exact fixed linear map, e.g. a
-// reduced-precision factorization); otherwise x += M^-1 (V y).
-int gmres_run(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const double2* A, const double2* rhs,
-              double2* x, int restart, int max_iter, double tol, int32_t* iters_out, double* resid_out,
-              cudaStream_t caller, Precond& M, bool flexible);
+// The operator of column c: either stored matrix cmat[c] of A ([nnz][Bm]), or a
+// matrix family sum_a coef[c][a] fam[a] (fam: [nfam][nnz], coef: [Bc][nfam], device)
+// formed on the fly inside the product, e.g. A(k) = E - k^2 B + sum_p gamma_p P_p.
+constexpr int kMaxFamily = 8;
+struct MatArg {
+    const double2* A = nullptr;
+    int64_t Bm = 0;
+    const int32_t* cmat = nullptr;
+    int nfam = 0;
+    const double2* fam = nullptr;
+    const double2* coef = nullptr;
+};
+
+// Y = A X, or Y = Bv - A X when Bv is not NULL (vectors [n][Bc]).
+void spmv_op(const emg_rplan* p, int64_t Bc, const MatArg& A, const double2* X, const double2* Bv, double2* Y,
+             cudaStream_t s);
+
+// Restarted GMRES(restart) with CGS2 over Bc lockstep columns.  flexible: keep
+// z_j = M^-1 v_j and update x with them (FGMRES, required when M^-1 is not an exact
+// fixed linear map, e.g. a reduced-precision factorization); otherwise
+// x += M^-1 (V y).
+int gmres_run(emg_rplan* p, int64_t Bc, const MatArg& A, const double2* rhs, double2* x, int restart, int max_iter,
+              double tol, int32_t* iters_out, double* resid_out, cudaStream_t caller, Precond& M, bool flexible);
+
+// Preconditioner on FP32 vectors (the inner solves of the mixed-precision refinement).
+struct Precond32 {
+    virtual ~Precond32() = default;
+    virtual int prepare(int64_t Bc) { (void)Bc; return EMG_OK; }
+    virtual int apply(const float2* in, float2* out, cudaStream_t s) = 0;   // in and out do not alias
+};
+
+// Mixed-precision solve: FP64 iterative refinement around inner FGMRES(restart)
+// iterations on FP32 vectors with the FP32 copy A32 of the stored matrices (same
+// [nnz][Bm] layout and cmat).  Each refinement step forms the true residual in
+// FP64, scales each column to unit norm, solves A32 d = r to ``inner_tol`` in FP32
+// and adds ||r|| d to x.  iters_out: inner iterations summed over the steps.
+int ir_run(emg_rplan* p, int64_t Bc, const MatArg& A, const float2* A32, const double2* rhs, double2* x, int restart,
+           int max_iter, double tol, double inner_tol, int32_t* iters_out, double* resid_out, int32_t* steps_out,
+           cudaStream_t caller, Precond32& M);
 
 }  // namespace emg

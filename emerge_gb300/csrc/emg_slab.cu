@@ -58,6 +58,7 @@ __device__ __forceinline__ double2 to_d(double2 v) { return v; }
 
 constexpr int kTile = 64;          // Gauss-Jordan tile and GEMM output tile
 constexpr int kThreads = 256;
+constexpr int kDiagThreads = 1024;  // pivot-tile inversion: 4 rows per thread
 constexpr int kMaxRows = 16;       // rows per CTA in the Schur-complement kernel
 constexpr int kSchurSmem = 200 * 1024;
 constexpr int64_t kMaxWidth = 12288;
@@ -204,9 +205,10 @@ __global__ void __launch_bounds__(kThreads) k_schur(int64_t wp, int64_t w, int64
 // the inverse also goes to pinv (ld 64).  Grid 1 x 1 x F.
 //
 // Gauss-Jordan on a 64 x 64 shared tile (padded with the identity when tb < 64),
-// two barriers per pivot.  Thread t owns column t % 64 and rows t / 64 + 4q, so a
-// warp touches 32 consecutive columns of one row (no bank conflicts).  Step c:
-// every thread reduces the four pivot candidates of column c (one per owner
+// two barriers per pivot.  Thread t owns column t % 64 and rows t / 64 + 16q, so a
+// warp touches 32 consecutive columns of one row (no bank conflicts); 1024 threads
+// keep enough warps per scheduler to hide the update's instruction latencies.  Step c:
+// every thread reduces the 16 pivot candidates of column c (one per owner
 // thread, largest |a_rc| below the diagonal, lowest row on ties); (S) the pivot
 // row p is swapped into row c while the scaled pivot row and the old column c are
 // formed; (U) rank-1 update from registers, during which the owners of column
@@ -218,19 +220,20 @@ template <typename T> __device__ __forceinline__ T crecip(T v) {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
+__global__ void __launch_bounds__(kDiagThreads) k_gj_diag(int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
                                                       int64_t totD, int64_t offD, typename C2<R>::T* __restrict__ pinv,
                                                       R rel_thr, int32_t* __restrict__ perturbed) {
     using T = typename C2<R>::T;
-    constexpr int kQ = kTile * kTile / kThreads;   // rows per thread (16)
+    constexpr int kQ = kTile * kTile / kDiagThreads;   // rows per thread
+    constexpr int kRowStep = kDiagThreads / kTile;     // row stride between a thread's rows
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T(*a)[kTile + 1] = reinterpret_cast<T(*)[kTile + 1]>(smem_raw);
     __shared__ T rowc[kTile], colc[kTile];
     __shared__ int piv[kTile], perm[kTile];
-    __shared__ R cand_m[kThreads / kTile];
-    __shared__ int cand_i[kThreads / kTile];
-    __shared__ T cand_v[kThreads / kTile];
-    __shared__ R s_red[kThreads / 32];
+    __shared__ R cand_m[kDiagThreads / kTile];
+    __shared__ int cand_i[kDiagThreads / kTile];
+    __shared__ T cand_v[kDiagThreads / kTile];
+    __shared__ R s_red[kDiagThreads / 32];
     const int64_t f = blockIdx.z;
     T* M = Sinv + f * totD + offD;
     const int64_t k0 = (int64_t)k * kTile;
@@ -238,7 +241,7 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int j = tid % kTile, r0 = tid / kTile, slot = r0;
     R mx = 0;
-    for (int idx = tid; idx < kTile * kTile; idx += kThreads) {
+    for (int idx = tid; idx < kTile * kTile; idx += kDiagThreads) {
         const int r = idx / kTile, c = idx % kTile;
         T v;
         if (r < tb && c < tb) {
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
     __syncthreads();
     R thr2 = 0;
 #pragma unroll
-    for (int i = 0; i < kThreads / 32; ++i) thr2 = max(thr2, s_red[i]);
+    for (int i = 0; i < kDiagThreads / 32; ++i) thr2 = max(thr2, s_red[i]);
     thr2 *= rel_thr * rel_thr;   // |pivot|^2 at or below this is replaced
     // candidates of column 0 from shared memory
     if (j == 0) {
@@ -264,7 +267,7 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
         T bv = mk((R)0, (R)0);
 #pragma unroll
         for (int q = 0; q < kQ; ++q) {
-            const int r = r0 + 4 * q;
+            const int r = r0 + kRowStep * q;
             if (r < tb) {
                 const T v = a[r][0];
                 const R m2 = v.x * v.x + v.y * v.y;
@@ -281,7 +284,7 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
         int p = cand_i[0];
         T pv = cand_v[0];
 #pragma unroll
-        for (int i = 1; i < kThreads / kTile; ++i) {
+        for (int i = 1; i < kDiagThreads / kTile; ++i) {
             const R m2 = cand_m[i];
             const int ii = cand_i[i];
             if (m2 > best || (m2 == best && ii < p)) { best = m2; p = ii; pv = cand_v[i]; }
@@ -304,10 +307,10 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
         __syncthreads();
         const T rj = rowc[j];
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) v[q] = a[r0 + 4 * q][j];
+        for (int q = 0; q < kQ; ++q) v[q] = a[r0 + kRowStep * q][j];
 #pragma unroll
         for (int q = 0; q < kQ; ++q) {
-            const int r = r0 + 4 * q;
+            const int r = r0 + kRowStep * q;
             const T cr = colc[r];
             if (r == c) {
                 v[q] = j == c ? inv : rj;
@@ -321,14 +324,14 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
             }
         }
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) a[r0 + 4 * q][j] = v[q];
+        for (int q = 0; q < kQ; ++q) a[r0 + kRowStep * q][j] = v[q];
         if (j == c + 1) {
             R bm = -1;
             int bi = kTile;
             T bv = mk((R)0, (R)0);
 #pragma unroll
             for (int q = 0; q < kQ; ++q) {
-                const int r = r0 + 4 * q;
+                const int r = r0 + kRowStep * q;
                 if (r > c && r < tb) {
                     const R m2 = v[q].x * v[q].x + v[q].y * v[q].y;
                     if (m2 > bm) { bm = m2; bi = r; bv = v[q]; }
@@ -347,7 +350,7 @@ __global__ void __launch_bounds__(kThreads) k_gj_diag(int64_t w, int k, typename
     }
     __syncthreads();
     T* P = pinv + f * kTile * kTile;
-    for (int idx = tid; idx < tb * tb; idx += kThreads) {
+    for (int idx = tid; idx < tb * tb; idx += kDiagThreads) {
         const int r = idx / tb, c = idx % tb;
         const T x = a[r][perm[c]];
         M[(k0 + r) * w + k0 + c] = x;
@@ -446,25 +449,70 @@ __global__ void __launch_bounds__(kThreads) k_sq_gemm(int64_t w, const typename 
         }
 }
 
-// ------------------------------------------------------------------- solve ---
+// Per-block partial sums of |R_ij - delta_ij|^2 over a w x w block per factor, then
+// their ordered total (deterministic): part[f][b], nrm2[f].
+constexpr int kNormBlocks = 64;
 template <typename R>
-__global__ void k_gather(int64_t n, int64_t Bc, const int32_t* __restrict__ perm, const double2* __restrict__ X,
+__global__ void k_dev_partial(int64_t w, const typename C2<R>::T* __restrict__ Rm, int64_t sq, double* __restrict__ part) {
+    const int64_t f = blockIdx.y;
+    const typename C2<R>::T* M = Rm + f * sq;
+    double acc = 0.0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < w * w; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / w, c = t % w;
+        const double x = (double)M[t].x - (r == c ? 1.0 : 0.0), y = (double)M[t].y;
+        acc += x * x + y * y;
+    }
+    __shared__ double red[kThreads];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = kThreads / 2; o; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[f * kNormBlocks + blockIdx.x] = red[0];
+}
+
+// X <- Xn for the factors whose refinement residual ||I - S X||_F is below 1/2
+// (Newton-Schulz only converges when the residual is below 1); counts the others.
+template <typename R>
+__global__ void k_copy_if(int64_t w, const typename C2<R>::T* __restrict__ Xn, int64_t sq, typename C2<R>::T* __restrict__ X,
+                          int64_t totD, const double* __restrict__ part, int32_t* __restrict__ skipped) {
+    const int64_t f = blockIdx.y;
+    double n2 = 0.0;
+    for (int b = 0; b < kNormBlocks; ++b) n2 += part[f * kNormBlocks + b];
+    if (!(n2 < 0.25)) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(skipped + f, 1);
+        return;
+    }
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < w * w; t += (int64_t)gridDim.x * blockDim.x)
+        X[f * totD + t] = Xn[f * sq + t];
+}
+
+// ------------------------------------------------------------------- solve ---
+__device__ __forceinline__ float2 as_t(float2 v, float2) { return v; }
+__device__ __forceinline__ float2 as_t(double2 v, float2) { return make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ double2 as_t(float2 v, double2) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 as_t(double2 v, double2) { return v; }
+
+// Y[pos] = X[perm[pos]] (restricted order -> slab order), converting the vector type
+template <typename R, typename TI>
+__global__ void k_gather(int64_t n, int64_t Bc, const int32_t* __restrict__ perm, const TI* __restrict__ X,
                          typename C2<R>::T* __restrict__ Y) {
     using T = typename C2<R>::T;
     const int64_t total = n * Bc;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t pos = t / Bc, c = t % Bc;
-        Y[t] = cvt<T>(X[(int64_t)perm[pos] * Bc + c]);
+        Y[t] = as_t(X[(int64_t)perm[pos] * Bc + c], T{});
     }
 }
 
-template <typename R>
+template <typename R, typename TI>
 __global__ void k_scatter(int64_t n, int64_t Bc, const int32_t* __restrict__ perm, const typename C2<R>::T* __restrict__ Z,
-                          double2* __restrict__ X) {
+                          TI* __restrict__ X) {
     const int64_t total = n * Bc;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t pos = t / Bc, c = t % Bc;
-        X[(int64_t)perm[pos] * Bc + c] = to_d(Z[t]);
+        X[(int64_t)perm[pos] * Bc + c] = as_t(Z[t], TI{});
     }
 }
 
@@ -491,6 +539,11 @@ __global__ void k_couple(int mode, int64_t w, int64_t row0, int64_t nb0, int64_t
 struct Group {
     int32_t fac, col0, ncol, pad;
 };
+
+__global__ void k_narrow(int64_t nv, const double2* __restrict__ in, float2* __restrict__ out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nv; t += (int64_t)gridDim.x * blockDim.x)
+        out[t] = make_float2((float)in[t].x, (float)in[t].y);
+}
 
 // Out[r, cols of group g] = beta Out + alpha S_i^-1[r, :] Y[:, cols]: warp per row,
 // lanes over the row of S_i^-1 (coalesced), 16 columns per pass.  Grid: row blocks x groups.
@@ -599,8 +652,8 @@ struct emg_slab {
     int prec = 0;                     // 1 complex FP32, 2 complex FP64
     int64_t F = 0;
     void *Sinv = nullptr, *Cval = nullptr, *Uval = nullptr, *UCval = nullptr, *pinv = nullptr;
-    int32_t* perturbed = nullptr;
-    int64_t n_perturbed = 0;
+    int32_t* perturbed = nullptr;     // [F] perturbed pivots, [F] skipped refinements
+    int64_t n_perturbed = 0, n_refine_skipped = 0;
     // solve workspace
     int64_t ws_cols = 0;
     size_t ws_bytes = 0;
@@ -809,6 +862,7 @@ extern "C" int emg_slab_info(const emg_slab* s, int64_t* info) {
     info[4] = s->F;
     info[5] = s->prec;
     info[6] = s->n_perturbed;
+    info[7] = s->n_refine_skipped;
     return EMG_OK;
 }
 
@@ -831,7 +885,7 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
     if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->Uval), F * std::max<int64_t>(s->nU, 1), "slab U values");
     if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->UCval), F * std::max<int64_t>(s->nU, 1), "slab U values (by column)");
     if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->pinv), F * kTile * kTile, "slab pivot tiles");
-    if (!rc) rc = dalloc(&s->perturbed, F, "slab pivot counters");
+    if (!rc) rc = dalloc(&s->perturbed, 2 * F, "slab pivot counters");
     if (rc) { slab_free_factors(s); return rc; }
     s->F = F;
     s->prec = sizeof(R) == 4 ? 1 : 2;
@@ -841,15 +895,20 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
     struct Tmp { int32_t* p; ~Tmp() { if (p) cudaFree(p); } } tmp{amat};
     // Newton-Schulz scratch: a copy of S_i and the factor 2I - S_i X (F blocks of maxw^2)
     T *Scopy = nullptr, *Rbuf = nullptr;
+    double* npart = nullptr;
     const int64_t sq = s->maxw * s->maxw;
     if (refine > 0) {
         rc = dalloc(&Scopy, F * sq, "slab refinement copy");
         if (!rc) rc = dalloc(&Rbuf, F * sq, "slab refinement factor");
-        if (rc) { dfree(Scopy); slab_free_factors(s); return rc; }
+        if (!rc) rc = dalloc(&npart, F * kNormBlocks, "slab refinement norms");
+        if (rc) { dfree(Scopy); dfree(Rbuf); slab_free_factors(s); return rc; }
     }
-    struct Tmp2 { T* a; T* b; ~Tmp2() { if (a) cudaFree(a); if (b) cudaFree(b); } } tmp2{Scopy, Rbuf};
+    struct Tmp2 {
+        T* a; T* b; double* c;
+        ~Tmp2() { if (a) cudaFree(a); if (b) cudaFree(b); if (c) cudaFree(c); }
+    } tmp2{Scopy, Rbuf, npart};
     EMG_CUDA(cudaMemcpyAsync(amat, amat_h, sizeof(int32_t) * F, cudaMemcpyHostToDevice, st));
-    EMG_CUDA(cudaMemsetAsync(s->perturbed, 0, sizeof(int32_t) * F, st));
+    EMG_CUDA(cudaMemsetAsync(s->perturbed, 0, sizeof(int32_t) * 2 * F, st));
     T* Sinv = static_cast<T*>(s->Sinv);
     EMG_CUDA(cudaMemsetAsync(Sinv, 0, sizeof(T) * F * s->totD, st));
     k_values<R><<<grid_for(s->nnz * F, 256), 256, 0, st>>>(s->nnz, Bm, F, amat, A, s->dmap, s->totD, Sinv);
@@ -882,7 +941,7 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
             EMG_CUDA(cudaMemcpy2DAsync(Scopy, sizeof(T) * sq, Sinv + s->offD[i], sizeof(T) * s->totD, sizeof(T) * w * w,
                                        (size_t)F, cudaMemcpyDeviceToDevice, st));
         for (int k = 0; k < nt; ++k) {
-            k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kThreads, diag_smem, st>>>(w, k, Sinv, s->totD, s->offD[i],
+            k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kDiagThreads, diag_smem, st>>>(w, k, Sinv, s->totD, s->offD[i],
                                                                              static_cast<T*>(s->pinv), rel_thr,
                                                                              s->perturbed);
             if (nt > 1) {
@@ -898,17 +957,22 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
             T* X = Sinv + s->offD[i];
             const dim3 g((unsigned)nt, (unsigned)nt, (unsigned)F);
             k_sq_gemm<R><<<g, kThreads, 0, st>>>(w, Scopy, sq, X, s->totD, Rbuf, sq, (R)-1, (R)2);
+            k_dev_partial<R><<<dim3(kNormBlocks, (unsigned)F), kThreads, 0, st>>>(w, Rbuf, sq, npart);
             k_sq_gemm<R><<<g, kThreads, 0, st>>>(w, X, s->totD, Rbuf, sq, Scopy, sq, (R)1, (R)0);
-            EMG_CUDA(cudaMemcpy2DAsync(X, sizeof(T) * s->totD, Scopy, sizeof(T) * sq, sizeof(T) * w * w, (size_t)F,
-                                       cudaMemcpyDeviceToDevice, st));
+            k_copy_if<R><<<dim3(grid_for(w * w, kThreads, 1024), (unsigned)F), kThreads, 0, st>>>(
+                w, Scopy, sq, X, s->totD, npart, s->perturbed + F);
         }
         EMG_CUDA(cudaGetLastError());
     }
-    std::vector<int32_t> pc(F);
-    EMG_CUDA(cudaMemcpyAsync(pc.data(), s->perturbed, sizeof(int32_t) * F, cudaMemcpyDeviceToHost, st));
+    std::vector<int32_t> pc(2 * F);
+    EMG_CUDA(cudaMemcpyAsync(pc.data(), s->perturbed, sizeof(int32_t) * 2 * F, cudaMemcpyDeviceToHost, st));
     EMG_CUDA(cudaStreamSynchronize(st));
     s->n_perturbed = 0;
-    for (auto v : pc) s->n_perturbed += v;
+    s->n_refine_skipped = 0;
+    for (int64_t f = 0; f < F; ++f) {
+        s->n_perturbed += pc[f];
+        s->n_refine_skipped += pc[F + f];
+    }
     return EMG_OK;
 }
 }  // namespace
@@ -964,8 +1028,8 @@ struct SlabPrecond : emg::Precond {
         EMG_CUDA(cudaMemcpy(s->groups, groups.data(), sizeof(emg::slab::Group) * groups.size(), cudaMemcpyHostToDevice));
         return EMG_OK;
     }
-    template <typename R>
-    int run(const double2* in, double2* out, cudaStream_t st) {
+    template <typename R, typename TI>
+    int run(const TI* in, TI* out, cudaStream_t st) {
         using namespace emg::slab;
         using T = typename C2<R>::T;
         T* Y = static_cast<T*>(s->Y);
@@ -986,7 +1050,7 @@ struct SlabPrecond : emg::Precond {
                 k_rowmv<R><<<dim3((unsigned)((w * 32 + kThreads - 1) / kThreads), G), kThreads, 0, st>>>(
                     w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, alpha, beta, Z);
         };
-        k_gather<R><<<grid_for(s->n * Bc, 256), 256, 0, st>>>(s->n, Bc, s->perm, in, Y);
+        k_gather<R, TI><<<grid_for(s->n * Bc, 256), 256, 0, st>>>(s->n, Bc, s->perm, in, Y);
         for (int i = 0; i < s->m; ++i) {
             const int64_t w = s->off[i + 1] - s->off[i];
             if (i > 0)
@@ -1000,13 +1064,22 @@ struct SlabPrecond : emg::Precond {
                                                                s->uidx, Uv, s->nU, Z, Y);
             dense(w, i, (R)-1, 1);
         }
-        k_scatter<R><<<grid_for(s->n * Bc, 256), 256, 0, st>>>(s->n, Bc, s->perm, Z, out);
+        k_scatter<R, TI><<<grid_for(s->n * Bc, 256), 256, 0, st>>>(s->n, Bc, s->perm, Z, out);
         EMG_CUDA(cudaGetLastError());
         return EMG_OK;
     }
     int apply(const double2* in, double2* out, cudaStream_t st) override {
-        return s->prec == 1 ? run<float>(in, out, st) : run<double>(in, out, st);
+        return s->prec == 1 ? run<float, double2>(in, out, st) : run<double, double2>(in, out, st);
     }
+};
+
+// The same slab solve on FP32 vectors (FP32 factors only), for the inner FGMRES of
+// the mixed-precision refinement.
+struct SlabPrecond32 : emg::Precond32 {
+    SlabPrecond base;
+    SlabPrecond32(emg_slab* s_, int64_t Bc_, const int32_t* cfac_) : base(s_, Bc_, cfac_) {}
+    int prepare(int64_t bc) override { return base.prepare(bc); }
+    int apply(const float2* in, float2* out, cudaStream_t st) override { return base.run<float, float2>(in, out, st); }
 };
 }  // namespace
 
@@ -1034,7 +1107,66 @@ extern "C" int emg_gmres_slab(const emg_rplan* pc, emg_slab* s, int64_t Bc, cons
     EMG_CHECK_ARG(s->F > 0, "emg_gmres_slab: no factorization");
     for (int64_t c = 0; c < Bc; ++c) EMG_CHECK_ARG(cfac[c] >= 0 && cfac[c] < s->F, "emg_gmres_slab: cfac out of range");
     SlabPrecond M(s, Bc, cfac);
-    return gmres_run(p, Bc, cmat, Bm, reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(rhs),
-                     reinterpret_cast<double2*>(x), restart, max_iter, tol, iters_out, resid_out, (cudaStream_t)stream, M,
-                     true);
+    MatArg Am;
+    Am.A = reinterpret_cast<const double2*>(A);
+    Am.Bm = Bm;
+    Am.cmat = cmat;
+    return gmres_run(p, Bc, Am, reinterpret_cast<const double2*>(rhs), reinterpret_cast<double2*>(x), restart, max_iter,
+                     tol, iters_out, resid_out, (cudaStream_t)stream, M, true);
+}
+
+extern "C" int emg_gmres_slab_family(const emg_rplan* pc, emg_slab* s, int64_t Bc, int nfam, const double* fam,
+                                     const double* coef, const int32_t* cfac, const double* rhs, double* x,
+                                     int restart, int max_iter, double tol, int32_t* iters_out, double* resid_out,
+                                     void* stream) {
+    using namespace emg;
+    emg_rplan* p = const_cast<emg_rplan*>(pc);
+    EMG_CHECK_ARG(p && s && s->rp == p && fam && coef && cfac && rhs && x && iters_out && resid_out && Bc > 0 &&
+                      nfam >= 1 && nfam <= kMaxFamily,
+                  "emg_gmres_slab_family: bad argument");
+    EMG_CHECK_ARG(restart >= 1 && restart <= 256 && max_iter >= 1 && tol > 0,
+                  "emg_gmres_slab_family: restart must be in [1, 256]");
+    EMG_CHECK_ARG(s->F > 0, "emg_gmres_slab_family: no factorization");
+    for (int64_t c = 0; c < Bc; ++c)
+        EMG_CHECK_ARG(cfac[c] >= 0 && cfac[c] < s->F, "emg_gmres_slab_family: cfac out of range");
+    SlabPrecond M(s, Bc, cfac);
+    MatArg Am;
+    Am.nfam = nfam;
+    Am.fam = reinterpret_cast<const double2*>(fam);
+    Am.coef = reinterpret_cast<const double2*>(coef);
+    return gmres_run(p, Bc, Am, reinterpret_cast<const double2*>(rhs), reinterpret_cast<double2*>(x), restart, max_iter,
+                     tol, iters_out, resid_out, (cudaStream_t)stream, M, true);
+}
+
+extern "C" int emg_gmres_slab_mixed(const emg_rplan* pc, emg_slab* s, int64_t Bc, const int32_t* cmat, int64_t Bm,
+                                    const double* A, const int32_t* cfac, const double* rhs, double* x, int restart,
+                                    int max_iter, double tol, double inner_tol, int32_t* iters_out, double* resid_out,
+                                    int32_t* steps_out, void* stream) {
+    using namespace emg;
+    emg_rplan* p = const_cast<emg_rplan*>(pc);
+    EMG_CHECK_ARG(p && s && s->rp == p && cmat && A && cfac && rhs && x && iters_out && resid_out && Bc > 0 && Bm > 0,
+                  "emg_gmres_slab_mixed: bad argument");
+    EMG_CHECK_ARG(restart >= 1 && restart <= 256 && max_iter >= 1 && tol > 0 && inner_tol > 0 && inner_tol < 1,
+                  "emg_gmres_slab_mixed: restart must be in [1, 256], tolerances in (0, 1)");
+    EMG_CHECK_ARG(s->F > 0 && s->prec == 1, "emg_gmres_slab_mixed: needs FP32 slab factors");
+    for (int64_t c = 0; c < Bc; ++c)
+        EMG_CHECK_ARG(cfac[c] >= 0 && cfac[c] < s->F, "emg_gmres_slab_mixed: cfac out of range");
+    if (p->ns == 0) return EMG_OK;
+    // FP32 copy of the stored matrices for the inner products
+    float2* A32 = nullptr;
+    int rc = dalloc(&A32, p->nnz * Bm, "mixed FP32 matrices");
+    if (rc) return rc;
+    struct Free { float2* a; ~Free() { if (a) cudaFree(a); } } fr{A32};
+    cudaStream_t st = (cudaStream_t)stream;
+    slab::k_narrow<<<grid_for(p->nnz * Bm, 256), 256, 0, st>>>(p->nnz * Bm, reinterpret_cast<const double2*>(A), A32);
+    EMG_CUDA(cudaGetLastError());
+    SlabPrecond32 M(s, Bc, cfac);
+    MatArg Am;
+    Am.A = reinterpret_cast<const double2*>(A);
+    Am.Bm = Bm;
+    Am.cmat = cmat;
+    rc = ir_run(p, Bc, Am, A32, reinterpret_cast<const double2*>(rhs), reinterpret_cast<double2*>(x), restart, max_iter,
+                tol, inner_tol, iters_out, resid_out, steps_out, st, M);
+    EMG_CUDA(cudaStreamSynchronize(st));   // A32 is freed on return
+    return rc;
 }

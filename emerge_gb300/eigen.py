@@ -7,9 +7,13 @@ sigma, which)``, and the 3-D cavity code path (fem/physics/edm/emfreq3d.py:
 PEC-restricted curl-curl (E) and mass (B) matrices, whose eigenvalues are k0^2.
 
 Method: shift-invert block Arnoldi on Op = (E - sigma B)^-1 B.  The shifted
-matrix is factored once with the slab factorization in complex FP32; every
-application of Op is an FGMRES solve to an FP64 residual of 1e-12 preconditioned
-by that factor (FP32 inner, FP64 refinement).  The Krylov basis is orthogonalised
+matrix is factored once with the slab factorization; every application of Op is
+an FGMRES solve to an FP64 relative residual of 1e-11 preconditioned by that
+factor.  The factor is complex FP64 by default: the shifted cavity operator is
+strongly indefinite (the curl-curl null space sits at -sigma B) and its FP32 slab
+inverses are too inaccurate to be a useful preconditioner on cube-like cavities
+(relative error of one application 0.6-1.5 against 0.1 on waveguides); FP32
+(``precision="fp32"``) still converges, with many more inner iterations.  The Krylov basis is orthogonalised
 (two classical Gram-Schmidt passes) and the Rayleigh-Ritz problem solved in FP64.
 B carries the reference's non-symmetric face-face mass block, so the pencil is
 not Hermitian and Arnoldi (not Lanczos) is used, as ``eigs`` does.  Ritz values
@@ -89,8 +93,8 @@ class ShiftInvertEigen:
         return W
 
     def solve(self, nmodes: int, sigma: float, which: str = "LR", block: int = 4, ncv: int | None = None,
-              tol: float = 1e-10, max_restarts: int = 30, precision: str = "fp32", seed: int = 0,
-              inner_tol: float = 1e-12, refine: int = 1, adapt: bool = False) -> EigResult:
+              tol: float = 1e-10, max_restarts: int = 30, precision: str = "fp64", seed: int = 0,
+              inner_tol: float = 1e-11, refine: int = 0, adapt: bool = False) -> EigResult:
         """nmodes eigenpairs; see the module docstring for ``which``.
 
         Thick-restarted block Arnoldi: after each Rayleigh-Ritz the wanted Ritz vectors

@@ -108,6 +108,17 @@ class RestrictedSystem:
                   _vp(Bv) if Bv is not None else None, _vp(Y), _stream())
         return Y
 
+    def spmv_family(self, fam, coef, X, Bv=None) -> torch.Tensor:
+        """Y = A_c X (or Bv - A_c X) with A_c = sum_a coef[c, a] fam[a] formed on the fly."""
+        X = X.contiguous()
+        fam = fam.contiguous()
+        coef = coef.contiguous()
+        Bv = None if Bv is None else Bv.contiguous()
+        Y = torch.empty(X.shape, dtype=X.dtype, device=X.device)
+        _lib.call("emg_spmv_family", self._plan, int(X.shape[1]), int(fam.shape[0]), _vp(fam), _vp(coef), _vp(X),
+                  _vp(Bv) if Bv is not None else None, _vp(Y), _stream())
+        return Y
+
     def gmres(self, A, LU, rhs, cmat, x0=None, restart=150, max_iter=20000, tol=1e-10):
         """Solve column c of rhs (n, Bc) with matrix cmat[c]; returns (x, iters, resid)."""
         Bc = int(rhs.shape[1])
@@ -169,11 +180,11 @@ class SlabFactor:
             self._h = None
 
     def info(self) -> dict:
-        v = np.zeros(7, dtype=np.int64)
+        v = np.zeros(8, dtype=np.int64)
         _lib.call("emg_slab_info", self._h, v.ctypes.data_as(ctypes.c_void_p))
         return {"slabs": int(v[0]), "max_width": int(v[1]), "dense_entries": int(v[2]), "couplings": int(v[3]),
                 "factors": int(v[4]), "precision": {0: None, 1: "fp32", 2: "fp64"}[int(v[5])],
-                "perturbed_pivots": int(v[6])}
+                "perturbed_pivots": int(v[6]), "refinements_skipped": int(v[7])}
 
     def levels(self):
         """(slab boundaries (slabs+1), restricted index of each slab position)."""
@@ -199,6 +210,41 @@ class SlabFactor:
         _lib.call("emg_slab_apply", self._h, int(X.shape[1]), cf.ctypes.data_as(ctypes.c_void_p), _vp(X), _vp(Y),
                   _stream())
         return Y
+
+    def gmres_family(self, fam, coef, rhs, cfac, x0=None, restart=40, max_iter=2000, tol=1e-10):
+        """FGMRES with column operators A_c = sum_a coef[c, a] fam[a] formed on the fly
+        (fam: (nfam, nnz_r), coef: (Bc, nfam) complex128 device tensors)."""
+        sysr = self.sys
+        Bc = int(rhs.shape[1])
+        cf = np.ascontiguousarray(cfac, dtype=np.int32)
+        rhs = rhs.contiguous()
+        fam = fam.contiguous()
+        coef = coef.contiguous()
+        x = torch.zeros(rhs.shape, dtype=rhs.dtype, device=rhs.device) if x0 is None else x0.contiguous().clone()
+        its = torch.zeros(Bc, dtype=torch.int32, device=sysr.device)
+        res = torch.zeros(Bc, dtype=torch.float64, device=sysr.device)
+        _lib.call("emg_gmres_slab_family", sysr._plan, self._h, Bc, int(fam.shape[0]), _vp(fam), _vp(coef),
+                  cf.ctypes.data_as(ctypes.c_void_p), _vp(rhs), _vp(x), int(restart), int(max_iter),
+                  ctypes.c_double(tol), _vp(its), _vp(res), _stream())
+        return x, its.cpu().numpy(), res.cpu().numpy()
+
+    def gmres_mixed(self, A, rhs, cmat, cfac, x0=None, restart=40, max_iter=2000, tol=1e-10, inner_tol=1e-6):
+        """Mixed precision (FP32 factors only): FP64 iterative refinement around FGMRES on
+        complex FP32 vectors.  Returns (x, inner iterations, residuals, refinement steps)."""
+        sysr = self.sys
+        Bc = int(rhs.shape[1])
+        cf = np.ascontiguousarray(cfac, dtype=np.int32)
+        rhs = rhs.contiguous()
+        A = A.contiguous()
+        x = torch.zeros(rhs.shape, dtype=rhs.dtype, device=rhs.device) if x0 is None else x0.contiguous().clone()
+        its = torch.zeros(Bc, dtype=torch.int32, device=sysr.device)
+        res = torch.zeros(Bc, dtype=torch.float64, device=sysr.device)
+        steps = ctypes.c_int32(0)
+        _lib.call("emg_gmres_slab_mixed", sysr._plan, self._h, Bc, _vp(cmat), int(A.shape[1]), _vp(A),
+                  cf.ctypes.data_as(ctypes.c_void_p), _vp(rhs), _vp(x), int(restart), int(max_iter),
+                  ctypes.c_double(tol), ctypes.c_double(inner_tol), _vp(its), _vp(res), ctypes.byref(steps),
+                  _stream())
+        return x, its.cpu().numpy(), res.cpu().numpy(), int(steps.value)
 
     def gmres(self, A, rhs, cmat, cfac, x0=None, restart=40, max_iter=2000, tol=1e-10):
         """FGMRES on column c of rhs with matrix cmat[c], preconditioned by factor cfac[c]."""
@@ -415,13 +461,21 @@ class FrequencySweep:
 
     def run_anchored(self, freqs, n_anchor: int = 4, anchors=None, precision: str = "fp32", tol: float = 1e-10,
                      restart: int = 40, max_iter: int = 2000, x0: torch.Tensor | None = None,
-                     chunk: int | None = None, refine: int = 0) -> SweepResult:
+                     chunk: int | None = None, refine: int = 0, operators: str = "stored",
+                     inner: str = "fp64") -> SweepResult:
         """Batched FGMRES sweep preconditioned by slab factorizations at anchor frequencies.
 
         Every (frequency, port) column runs FP64 FGMRES to ``tol`` on its own A(k),
         preconditioned by the factor of the nearest anchor; with ``precision="fp32"``
         the factors and their solves are complex FP32 (mixed precision: FP32 inner,
-        FP64 residuals and updates)."""
+        FP64 residuals and updates).  ``operators``: "stored" forms A(k) for every
+        frequency of a chunk (16 nnz_r bytes per frequency; one complex FP64 MAC per
+        nonzero and column in the products); "family" keeps only E, B and the port
+        matrices and forms A(k) inside every product (2 + n_ports MACs per nonzero
+        and column: slower on GB300's FP64 pipes, for when memory is short).
+        ``inner="fp32"`` (FP32 factors, stored operators): FP64 iterative refinement
+        around FGMRES on complex FP32 vectors and an FP32 copy of A(k); the
+        iteration counts are then inner iterations summed over refinement steps."""
         freqs = np.asarray(freqs, dtype=float)
         nf, npo = len(freqs), len(self.ports)
         anchors = self.default_anchors(freqs, n_anchor) if anchors is None else np.asarray(anchors, dtype=float)
@@ -435,21 +489,39 @@ class FrequencySweep:
         its = np.zeros(nf * npo, dtype=np.int64)
         res = np.zeros(nf * npo)
         chunk = chunk or nf
+        steps = 0
+        fam = self.family() if operators == "family" else None
+        # column coefficients of A(k) = E - k^2 B + sum_p gamma_p P_p, one row per frequency
+        cf = np.zeros((nf, 2 + gam.shape[0]), dtype=np.complex128)
+        cf[:, 0] = 1.0
+        cf[:, 1] = -k0 ** 2
+        cf[:, 2:] = gam.T
         for f0 in range(0, nf, chunk):
             f1 = min(nf, f0 + chunk)
-            A = sysr.form(self.E, self.B, k0[f0:f1] ** 2, self.P, gam[:, f0:f1])
             rhs = self._rhs(beta[:, f0:f1])
-            cmat = torch.arange(f1 - f0, dtype=torch.int32, device=self.device).repeat_interleave(npo)
             cfac = np.repeat(near[f0:f1], npo)
             xin = None if x0 is None else x0[:, f0 * npo:f1 * npo]
-            x, it, rs = sl.gmres(A, rhs, cmat, cfac, x0=xin, restart=restart, max_iter=max_iter, tol=tol)
+            if operators == "family":
+                coef = torch.as_tensor(np.repeat(cf[f0:f1], npo, axis=0), device=self.device)
+                x, it, rs = sl.gmres_family(fam, coef, rhs, cfac, x0=xin, restart=restart, max_iter=max_iter, tol=tol)
+            else:
+                A = sysr.form(self.E, self.B, k0[f0:f1] ** 2, self.P, gam[:, f0:f1])
+                cmat = torch.arange(f1 - f0, dtype=torch.int32, device=self.device).repeat_interleave(npo)
+                if inner == "fp32" and precision == "fp32":
+                    x, it, rs, nsteps = sl.gmres_mixed(A, rhs, cmat, cfac, x0=xin, restart=restart,
+                                                       max_iter=max_iter, tol=tol)
+                    steps = max(steps, nsteps)
+                else:
+                    x, it, rs = sl.gmres(A, rhs, cmat, cfac, x0=xin, restart=restart, max_iter=max_iter, tol=tol)
+                del A
             X[:, f0 * npo:f1 * npo] = x
             its[f0 * npo:f1 * npo] = it
             res[f0 * npo:f1 * npo] = rs
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
         S = self._sparams(X, nf, beta)
-        info = {"anchors": anchors, "precision": precision, "refine": refine, "factor_seconds": t_fac, **sl.info()}
+        info = {"anchors": anchors, "precision": precision, "refine": refine, "inner": inner,
+                "refinement_steps": steps, "factor_seconds": t_fac, **sl.info()}
         return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X, info)
 
     def run(self, freqs, method: str = "batched", tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
@@ -503,6 +575,14 @@ class FrequencySweep:
         S = self._sparams(X, nf, beta)
         return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X)
 
+
+    def family(self) -> torch.Tensor:
+        """(2 + n_robin, nnz_r) restricted values of E, B and the unit port matrices: the
+        matrix family whose combination (1, -k^2, gamma_1(k), ...) is A(k)."""
+        if getattr(self, "_fam", None) is None:
+            Er, Br, Pr = self._restricted_parts()
+            self._fam = torch.stack([Er[:, 0], Br[:, 0]] + [P[:, 0] for P in Pr]).contiguous()
+        return self._fam
 
     # ------------------------------------------------------------ warm start ---
     def _restricted_parts(self):
@@ -583,7 +663,7 @@ class FrequencySweep:
 
     def run_warm(self, freqs, n_train: int = 32, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
                  chunk: int | None = None, guess: str = "projection", solver: str = "ilu0", n_anchor: int = 4,
-                 precision: str = "fp32", mlp_steps: int = 1500, refine: int = 0) -> SweepResult:
+                 precision: str = "fp32", mlp_steps: int = 1500, refine: int = 0, inner: str = "fp64") -> SweepResult:
         """Batched sweep: solve n_train evenly spread points, build an initial guess for
         every point from their span (``guess`` = "projection": minimal residual;
         "mlp": the warm-start network; "none": zero), then finish all points with
@@ -598,7 +678,7 @@ class FrequencySweep:
             anchors = self.default_anchors(freqs, n_anchor)
             solve = lambda fr, x0=None: self.run_anchored(fr, anchors=anchors, precision=precision, tol=tol,  # noqa: E731
                                                            restart=min(restart, 60), max_iter=max_iter, x0=x0,
-                                                           chunk=chunk, refine=refine)
+                                                           chunk=chunk, refine=refine, inner=inner)
         else:
             solve = lambda fr, x0=None: self.run(fr, method="batched", tol=tol, restart=restart,  # noqa: E731
                                                  max_iter=max_iter, x0=x0, chunk=chunk)

@@ -156,6 +156,14 @@ int emg_ilu_apply(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_
 int emg_spmv(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A, const double* X,
              const double* Bv, double* Y, void* stream);
 
+/* Y = A_c X (or Bv - A_c X) with the column operator formed on the fly from a
+ * matrix family: A_c = sum_a coef[c][a] fam[a], fam [nfam][nnz_r], coef [Bc][nfam]
+ * (complex, DEVICE), nfam <= 8.  A frequency sweep's A(k) = E - k^2 B +
+ * sum_p gamma_p(k) P_p is the family (E, B, P_1, ...) with coefficients
+ * (1, -k^2, gamma_1, ...): one copy of the matrices serves every frequency. */
+int emg_spmv_family(const emg_rplan* plan, int64_t Bc, int nfam, const double* fam, const double* coef,
+                    const double* X, const double* Bv, double* Y, void* stream);
+
 /* out[i][c] = full[c][solve_ids[i]] (full: Bc vectors of N) and the inverse
  * scatter (zeros on removed DOFs). */
 int emg_rplan_gather(const emg_rplan* plan, int64_t Bc, const double* full, double* out, void* stream);
@@ -187,16 +195,18 @@ typedef struct emg_slab emg_slab;
  * EMG_ERR_LIMIT if a slab is wider than 12288 DOFs. */
 int emg_slab_create(const emg_rplan* plan, int64_t n_seeds, const int64_t* seeds, void* stream, emg_slab** slab);
 void emg_slab_destroy(emg_slab* slab);
-/* info[7] (host): slabs, widest slab, dense entries per factor, coupling entries,
- * factors held, precision, perturbed pivots of the last factorization. */
+/* info[8] (host): slabs, widest slab, dense entries per factor, coupling entries,
+ * factors held, precision, perturbed pivots and skipped refinements (slabs whose
+ * ||I - S X||_F was not below 1/2) of the last factorization. */
 int emg_slab_info(const emg_slab* slab, int64_t* info);
 /* HOST outputs: slab boundaries off_out (slabs+1) and, if not NULL, perm_out
  * (n_solve): restricted index of each slab position. */
 int emg_slab_levels(const emg_slab* slab, int64_t* off_out, int32_t* perm_out);
 /* Factor the F matrices A[:, amat[f]] (A: [nnz_r][Bm] complex, DEVICE; amat: F
  * HOST int32).  refine = 1 applies one Newton-Schulz step X <- X (2I - S X) to
- * every slab inverse (two extra dense products; recovers most of the accuracy
- * that inverting without pivoting across 64-row tiles loses); 0 = none.
+ * every slab inverse whose residual ||I - S X||_F is below 1/2 (two extra dense
+ * products; recovers most of the accuracy that inverting without pivoting across
+ * 64-row tiles loses); 0 = none.
  * Replaces any factorization held.  Synchronises ``stream``. */
 int emg_slab_factor(emg_slab* slab, int precision, int64_t F, const int32_t* amat, int64_t Bm, const double* A,
                     int refine, void* stream);
@@ -210,6 +220,22 @@ int emg_slab_apply(emg_slab* slab, int64_t Bc, const int32_t* cfac, const double
 int emg_gmres_slab(const emg_rplan* plan, emg_slab* slab, int64_t Bc, const int32_t* cmat, int64_t Bm, const double* A,
                    const int32_t* cfac, const double* rhs, double* x, int restart, int max_iter, double tol,
                    int32_t* iters_out, double* resid_out, void* stream);
+
+/* Mixed-precision solve with FP32 slab factors: FP64 iterative refinement (true
+ * residual b - A x in FP64 each step) around an inner FGMRES on complex FP32
+ * vectors with an FP32 copy of A (made inside, nnz_r * Bm * 8 bytes), run to the
+ * relative tolerance inner_tol per step.  iters_out: inner iterations summed over
+ * the steps; *steps_out (HOST, may be NULL): refinement steps. */
+int emg_gmres_slab_mixed(const emg_rplan* plan, emg_slab* slab, int64_t Bc, const int32_t* cmat, int64_t Bm,
+                         const double* A, const int32_t* cfac, const double* rhs, double* x, int restart, int max_iter,
+                         double tol, double inner_tol, int32_t* iters_out, double* resid_out, int32_t* steps_out,
+                         void* stream);
+
+/* emg_gmres_slab with the operators of a matrix family (see emg_spmv_family)
+ * instead of stored matrices. */
+int emg_gmres_slab_family(const emg_rplan* plan, emg_slab* slab, int64_t Bc, int nfam, const double* fam,
+                          const double* coef, const int32_t* cfac, const double* rhs, double* x, int restart,
+                          int max_iter, double tol, int32_t* iters_out, double* resid_out, void* stream);
 
 /* ------------------------------------------------------ warm-start MLP ---
  * No counterpart in the reference (a sweep acceleration).  A multilayer

@@ -153,3 +153,20 @@ def test_wide_column_groups_use_tiled_product(system):
     for c in (0, 59, 65):
         ref = spla.spsolve(Ks[0 if c < 60 else 1].tocsc(), B[:, c])
         assert np.linalg.norm(wide[:, c] - ref) / np.linalg.norm(ref) <= 1e-9
+
+
+def test_mixed_precision_refinement_reaches_fp64_accuracy(system):
+    """FP64 iterative refinement around FGMRES on complex FP32 vectors (FP32 factors,
+    FP32 copy of A): FP64 residual 1e-10 and SuperLU's solution within 1e-7."""
+    torch, sysr, slab, Ks, rhs, vals = system
+    slab.factor(vals, [0, 1], "fp32")
+    B = np.concatenate(rhs, axis=1)
+    Bt = torch.as_tensor(B, device="cuda")
+    cmat = torch.tensor([0, 0, 1, 1], dtype=torch.int32, device="cuda")
+    x, its, res, steps = slab.gmres_mixed(vals, Bt, cmat, [0, 0, 1, 0], tol=1e-10, restart=40, max_iter=400)
+    assert np.all(res <= 1e-10)
+    assert 2 <= steps <= 6
+    x = x.cpu().numpy()
+    for c in range(4):
+        ref = spla.spsolve(Ks[c // 2].tocsc(), B[:, c])
+        assert np.linalg.norm(x[:, c] - ref) / np.linalg.norm(ref) <= 1e-7

@@ -91,3 +91,24 @@ def test_mlp_warm_start_saves_iterations_over_cold_start(waveguide):
     assert np.max(np.abs(warm.S - cold.S)) <= 1e-6
     assert warm.info["mlp_loss"] < 1e-2
     assert warm.iterations.sum() < cold.iterations.sum()
+
+
+def test_matrix_family_product_equals_formed_matrices(waveguide):
+    """A(k) X from the family (E, B, P_1, P_2) with coefficients (1, -k^2, gamma_p) equals
+    the product with the formed restricted matrices (emg_rplan_form)."""
+    import torch
+    from emerge_gb300.solver import FrequencySweep
+    z, field, bcs, eye, asm = waveguide
+    sw = FrequencySweep(asm, field, eye, eye, bcs)
+    freqs = np.array([8.7e9, 9.9e9, 11.3e9])
+    k0, gam, beta = sw._coeffs(freqs)
+    A = sw.sys.form(sw.E, sw.B, k0 ** 2, sw.P, gam)
+    fam = sw.family()
+    coef = np.zeros((len(freqs), fam.shape[0]), dtype=np.complex128)
+    coef[:, 0], coef[:, 1], coef[:, 2:] = 1.0, -k0 ** 2, gam.T
+    rng = np.random.default_rng(3)
+    X = torch.as_tensor(rng.standard_normal((sw.sys.n, 3)) + 1j * rng.standard_normal((sw.sys.n, 3)), device="cuda")
+    cm = torch.arange(3, dtype=torch.int32, device="cuda")
+    ref = sw.sys.spmv(A, X, cm)
+    got = sw.sys.spmv_family(fam, torch.as_tensor(coef, device="cuda"), X)
+    assert (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item() <= 1e-13
