@@ -261,6 +261,9 @@ def run_gpu(args, rank, world):
         del E, B, pin_E, pin_B, npE, npB, plan
         torch.cuda.empty_cache()
         out["sweep"] = run_sweep(args)
+    if rank == 0 and args.eigen > 0:
+        torch.cuda.empty_cache()
+        out["eigen"] = run_eigen(args)
     if rank == 0 and not args.no_cpu:
         nts, ti, tc = cpu_reference(field, er_s, args.cpu_sample)
         out["cpu_baseline"] = {"value": nts / (ti + tc), "unit": "tets/s", "cores": os.cpu_count(), "kind": "port",
@@ -312,11 +315,13 @@ def run_sweep(args):
         sw.run_warm(freqs[:4], n_train=2, solver="anchored", n_anchor=1, precision="fp32", guess="mlp",
                     tol=args.sweep_tol, mlp_steps=50)
         sw._slab_key = None
+        kw = dict(precision="fp32", tol=args.sweep_tol, restart=args.sweep_restart, chunk=chunk,
+                  refine=args.sweep_refine, inner=args.sweep_inner)
         fast = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored", n_anchor=args.sweep_anchors,
-                           precision="fp32", guess="mlp", tol=args.sweep_tol, restart=args.sweep_restart,
-                           chunk=chunk, mlp_steps=args.sweep_mlp_steps)
-        cold = sw.run_anchored(freqs, n_anchor=args.sweep_anchors, precision="fp32", tol=args.sweep_tol,
-                               restart=args.sweep_restart, chunk=chunk)
+                           guess="mlp", mlp_steps=args.sweep_mlp_steps, **kw)
+        proj = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored", n_anchor=args.sweep_anchors,
+                           guess="projection", **kw)
+        cold = sw.run_anchored(freqs, n_anchor=args.sweep_anchors, **kw)
         plain = sw.run(freqs[idx], method="plain", precond="slab64", tol=args.sweep_tol)
     v_fast = nf / fast.seconds
     v_plain = len(idx) / plain.seconds
@@ -333,6 +338,10 @@ def run_sweep(args):
         "iterations_fast_mean": float(fast.iterations.mean()), "iterations_fast_max": int(fast.iterations.max()),
         "iterations_cold_mean": float(cold.iterations.mean()), "cold_pts_per_s": nf / cold.seconds,
         "max_abs_dS_cold_vs_fast": float(np.max(np.abs(cold.S - fast.S))),
+        "projection_pts_per_s": nf / proj.seconds, "iterations_projection_mean": float(proj.iterations.mean()),
+        "max_abs_dS_projection_vs_plain": float(np.max(np.abs(proj.S[idx] - plain.S))),
+        "inner": args.sweep_inner, "refine": args.sweep_refine,
+        "refinement_steps": int(fast.info.get("refinement_steps", 0)),
         "iterations_plain_mean": float(plain.iterations.mean()),
         "S21_db_samples": [round(float(20 * np.log10(abs(v) + 1e-300)), 2) for v in fast.S[::max(1, nf // 8), 1, 0]],
         "clocks": clk.summary(),
@@ -345,6 +354,58 @@ def run_sweep(args):
                                    "converged": bool(ilu.residuals.max() <= args.sweep_tol * 10)}
     if args.sweep_cpu > 0:
         out["cpu_superlu"] = cpu_superlu(sw, freqs[idx[:args.sweep_cpu]], plain)
+    return out
+
+
+def run_eigen(args):
+    """Cavity eigenmodes: the smallest ``--eigen`` instances of the seeded 64-cavity batch
+    (sides U[15,40] mm, dielectric cylinder r U[2,6] mm, eps U[2,30], h = 2.2 mm), 10
+    lowest nonzero modes each, one instance after another.  The first instance is
+    checked against SciPy ARPACK (eigs, shift-invert, the reference's method) on the
+    host: max relative eigenvalue error."""
+    import scipy.sparse as sps
+    import scipy.sparse.linalg as spla
+    import torch
+    from emerge_gb300.eigen import CavityEigen, box_sigma
+    from emerge_gb300.freq import Assembler
+    from emerge_gb300.geometry import cavity_set
+    ps = cavity_set(64, seed=4, h=args.eigen_h)
+    order = sorted(range(64), key=lambda i: ps[i].field.n_field)[: args.eigen]
+    asm = Assembler()
+    out = {"workload": f"{len(order)} smallest of 64 seeded PEC cavities with dielectric cylinders, h={args.eigen_h}",
+           "modes": args.eigen_modes, "instances": []}
+    total = 0.0
+    err = None
+    with ClockSampler(0) as clk:
+        for k, i in enumerate(order):
+            p = ps[i]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ce = CavityEigen(asm, p.field, p.er, p.ur, p.bcs)
+            nodes = np.asarray(p.mesh.nodes)
+            dims = nodes.max(axis=1) - nodes.min(axis=1)
+            sigma = box_sigma(dims, float(np.max(np.abs(p.er[0, 0]))))
+            r = ce.solve(args.eigen_modes, sigma=sigma, which="LR", tol=1e-10)
+            torch.cuda.synchronize()
+            secs = time.perf_counter() - t0
+            total += secs
+            out["instances"].append({"n": int(ce.sys.n), "seconds": round(secs, 2), "max_residual": float(r.residuals.max()),
+                                     "restarts": r.info["restarts"], "solves": r.info["solves"],
+                                     "slabs": r.info["slabs"], "max_slab_width": r.info["max_width"],
+                                     "f_GHz": [round(float(f) / 1e9, 5) for f in r.frequencies[:3]]})
+            if k == 0 and args.eigen_check:
+                ptr, ind = ce.sys.pattern()
+                n = ce.sys.n
+                E = sps.csc_matrix(sps.csr_matrix((ce.Er[:, 0].cpu().numpy(), ind, ptr), shape=(n, n)))
+                B = sps.csc_matrix(sps.csr_matrix((ce.Br[:, 0].cpu().numpy(), ind, ptr), shape=(n, n)))
+                t1 = time.perf_counter()
+                ref = np.sort(spla.eigs(E, k=args.eigen_modes, M=B, sigma=sigma, which="LR", tol=1e-13)[0].real)
+                out["arpack_seconds"] = round(time.perf_counter() - t1, 2)
+                err = float(np.max(np.abs(np.sort(r.eigenvalues.real) - ref) / ref))
+            del ce
+            asm._dev = None
+    out.update({"seconds_total": round(total, 2), "instances_per_s": len(order) / total,
+                "max_rel_eig_error_vs_arpack": err, "clocks": clk.summary()})
     return out
 
 
@@ -397,11 +458,19 @@ def main():
     ap.add_argument("--sweep-restart", type=int, default=40)
     ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: all)")
     ap.add_argument("--sweep-mlp-steps", type=int, default=1500)
+    ap.add_argument("--sweep-inner", default="fp32", choices=["fp32", "fp64"],
+                    help="precision of the inner Krylov vectors of the fast sweep")
+    ap.add_argument("--sweep-refine", type=int, default=1, help="Newton-Schulz step on the FP32 slab inverses")
     ap.add_argument("--sweep-plain", type=int, default=2)
     ap.add_argument("--sweep-ilu-iters", type=int, default=1000)
     ap.add_argument("--sweep-cpu", type=int, default=1, help="points solved by SciPy SuperLU on the host")
     ap.add_argument("--sweep-tol", type=float, default=1e-8)
     ap.add_argument("--sweep-only", action="store_true", help="print only the sweep measurement")
+    ap.add_argument("--eigen", type=int, default=2, help="cavity eigen instances (0: skip)")
+    ap.add_argument("--eigen-h", type=float, default=2.2e-3)
+    ap.add_argument("--eigen-modes", type=int, default=10)
+    ap.add_argument("--eigen-check", type=int, default=1, help="ARPACK check of the first instance")
+    ap.add_argument("--eigen-only", action="store_true", help="print only the eigen measurement")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -417,6 +486,9 @@ def main():
     elif args.sweep_only:
         if rank == 0:
             print(json.dumps(run_sweep(args)))
+    elif args.eigen_only:
+        if rank == 0:
+            print(json.dumps(run_eigen(args)))
     else:
         run_gpu(args, rank, world)
     if world > 1:
