@@ -458,8 +458,8 @@ def main():
     ap.add_argument("--sweep-restart", type=int, default=40)
     ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: all)")
     ap.add_argument("--sweep-mlp-steps", type=int, default=1500)
-    ap.add_argument("--sweep-inner", default="fp32", choices=["fp32", "fp64"],
-                    help="precision of the inner Krylov vectors of the fast sweep")
+    ap.add_argument("--sweep-inner", default="fp64", choices=["fp32", "fp64"],
+                    help="precision of the Krylov vectors of the fast sweep (its factors are FP32 either way)")
     ap.add_argument("--sweep-refine", type=int, default=1, help="Newton-Schulz step on the FP32 slab inverses")
     ap.add_argument("--sweep-plain", type=int, default=2)
     ap.add_argument("--sweep-ilu-iters", type=int, default=1000)

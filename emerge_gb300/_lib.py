@@ -54,7 +54,7 @@ SIGNATURES = {
                                              ctypes.c_int, ctypes.c_int, ctypes.c_double, c_vp, c_vp, c_vp]),
     "emg_gmres_slab_mixed": (ctypes.c_int, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_double, ctypes.c_double, c_vp, c_vp, c_vp, c_vp]),
-    "emg_slab_create": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, ctypes.POINTER(c_vp)]),
+    "emg_slab_create": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, ctypes.POINTER(c_vp)]),
     "emg_slab_destroy": (None, [c_vp]),
     "emg_slab_info": (ctypes.c_int, [c_vp, c_vp]),
     "emg_slab_levels": (ctypes.c_int, [c_vp, c_vp, c_vp]),

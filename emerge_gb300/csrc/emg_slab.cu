@@ -713,8 +713,8 @@ std::vector<int64_t> bfs(const std::vector<int64_t>& starts, const std::vector<i
 }
 }  // namespace
 
-extern "C" int emg_slab_create(const emg_rplan* rp, int64_t n_seeds, const int64_t* seeds, void* stream,
-                               emg_slab** out) {
+extern "C" int emg_slab_create(const emg_rplan* rp, int64_t n_seeds, const int64_t* seeds, const int64_t* order_key,
+                               void* stream, emg_slab** out) {
     using namespace emg;
     EMG_CHECK_ARG(rp && out && n_seeds >= 0 && (n_seeds == 0 || seeds), "emg_slab_create: NULL argument");
     for (int64_t i = 0; i < n_seeds; ++i)
@@ -778,10 +778,21 @@ extern "C" int emg_slab_create(const emg_rplan* rp, int64_t n_seeds, const int64
         set_error("emg_slab_create: a slab is wider than 12288 DOFs (structure not slab-like)");
         return EMG_ERR_LIMIT;
     }
-    // positions: slabs in order, restricted index ascending inside a slab
+    // positions: slabs in order; inside a slab ascending order_key (then restricted
+    // index), or restricted index without a key.  The order decides which DOFs share
+    // a 64 x 64 pivot tile of the slab inverse, and with it the FP32 accuracy: a
+    // spatially local order with the two DOFs of an entity adjacent keeps strongly
+    // coupled DOFs in the same tile.
     std::vector<int32_t> perm(n);
     std::vector<int64_t> ipos(n), fill(s->off.begin(), s->off.end() - 1);
-    for (int64_t v = 0; v < n; ++v) {
+    std::vector<int64_t> vs(n);
+    for (int64_t v = 0; v < n; ++v) vs[v] = v;
+    std::stable_sort(vs.begin(), vs.end(), [&](int64_t a, int64_t b) {
+        if (lev[a] != lev[b]) return lev[a] < lev[b];
+        if (order_key && order_key[a] != order_key[b]) return order_key[a] < order_key[b];
+        return a < b;
+    });
+    for (int64_t v : vs) {
         const int64_t p = fill[lev[v]]++;
         perm[p] = (int32_t)v;
         ipos[v] = p;

@@ -33,7 +33,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from .solver import RestrictedSystem, SlabFactor, face_seeds
+from .solver import RestrictedSystem, SlabFactor, face_seeds, locality_key
 
 
 @dataclass
@@ -208,7 +208,7 @@ class CavityEigen:
         self.Br = self.sys.form(z, B, [-1.0])
         nodes = np.asarray(fieldb.mesh.nodes)
         axis = int(np.argmax(nodes.max(axis=1) - nodes.min(axis=1)))
-        self.slab = SlabFactor(self.sys, face_seeds(fieldb, self.solve_ids, axis))
+        self.slab = SlabFactor(self.sys, face_seeds(fieldb, self.solve_ids, axis), locality_key(fieldb, self.solve_ids))
         self.eig = ShiftInvertEigen(self.sys, self.Er, self.Br, self.slab)
 
     def solve(self, nmodes: int = 10, sigma: float | None = None, **kw) -> EigResult:

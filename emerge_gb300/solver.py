@@ -145,6 +145,37 @@ def dof_positions(field) -> np.ndarray:
     return np.concatenate([e_mid, f_mid, e_mid, f_mid], axis=1)
 
 
+def _morton3(q: np.ndarray) -> np.ndarray:
+    """Interleaved bits of three 21-bit non-negative integer coordinates (3, n)."""
+    def spread(x):
+        x = x.astype(np.uint64) & np.uint64(0x1FFFFF)
+        x = (x | (x << np.uint64(32))) & np.uint64(0x1F00000000FFFF)
+        x = (x | (x << np.uint64(16))) & np.uint64(0x1F0000FF0000FF)
+        x = (x | (x << np.uint64(8))) & np.uint64(0x100F00F00F00F00F)
+        x = (x | (x << np.uint64(4))) & np.uint64(0x10C30C30C30C30C3)
+        x = (x | (x << np.uint64(2))) & np.uint64(0x1249249249249249)
+        return x
+    return spread(q[0]) | (spread(q[1]) << np.uint64(1)) | (spread(q[2]) << np.uint64(2))
+
+
+def locality_key(field, solve_ids) -> np.ndarray:
+    """Rank of every kept DOF in a Z-order (Morton) walk over its entity's position,
+    with the two DOFs of an edge or face next to each other: the order of the DOFs
+    inside a slab (see SlabFactor)."""
+    sid = np.asarray(solve_ids, dtype=np.int64)
+    pos = dof_positions(field)[:, sid]
+    lo = pos.min(axis=1, keepdims=True)
+    hi = pos.max(axis=1, keepdims=True)
+    q = np.round((pos - lo) / np.maximum(hi - lo, 1e-30) * (2 ** 20)).astype(np.int64)
+    nE, nF = int(np.asarray(field.mesh.edges).shape[1]), int(np.asarray(field.mesh.tris).shape[1])
+    second = sid >= nE + nF
+    entity = np.where(second, sid - nE - nF, sid)
+    order = np.lexsort((second.astype(np.int64), entity, _morton3(q)))
+    key = np.empty(sid.size, dtype=np.int64)
+    key[order] = np.arange(sid.size, dtype=np.int64)
+    return key
+
+
 def face_seeds(field, solve_ids, axis: int) -> np.ndarray:
     """Restricted indices of the kept DOFs with the smallest coordinate along ``axis``:
     the start set of a slab search whose slabs are then cross-sections normal to it."""
@@ -161,13 +192,16 @@ class SlabFactor:
     matrices at once, in complex FP32 (``"fp32"``) or FP64 (``"fp64"``).
     """
 
-    def __init__(self, sysr: RestrictedSystem, seeds=None):
+    def __init__(self, sysr: RestrictedSystem, seeds=None, order_key=None):
         self.sys = sysr
         self._lib = sysr._lib
         h = ctypes.c_void_p()
         sd = np.ascontiguousarray(np.zeros(0) if seeds is None else seeds, dtype=np.int64)
+        key = None if order_key is None else np.ascontiguousarray(order_key, dtype=np.int64)
+        if key is not None and key.size != sysr.n:
+            raise ValueError("SlabFactor: order_key needs one entry per restricted DOF")
         _lib.call("emg_slab_create", sysr._plan, int(sd.size), sd.ctypes.data_as(ctypes.c_void_p) if sd.size else None,
-                  _stream(), ctypes.byref(h))
+                  key.ctypes.data_as(ctypes.c_void_p) if key is not None else None, _stream(), ctypes.byref(h))
         self._h = h
 
     def __del__(self):
@@ -228,7 +262,7 @@ class SlabFactor:
                   ctypes.c_double(tol), _vp(its), _vp(res), _stream())
         return x, its.cpu().numpy(), res.cpu().numpy()
 
-    def gmres_mixed(self, A, rhs, cmat, cfac, x0=None, restart=40, max_iter=2000, tol=1e-10, inner_tol=1e-6):
+    def gmres_mixed(self, A, rhs, cmat, cfac, x0=None, restart=40, max_iter=2000, tol=1e-10, inner_tol=1e-4):
         """Mixed precision (FP32 factors only): FP64 iterative refinement around FGMRES on
         complex FP32 vectors.  Returns (x, inner iterations, residuals, refinement steps)."""
         sysr = self.sys
@@ -431,7 +465,7 @@ class FrequencySweep:
                 u = self.u[self.ports[0].port_number].abs().cpu().numpy()
                 on_port = np.flatnonzero(u[self.solve_ids] > 0)
                 seeds = on_port if on_port.size else None
-            self._slab = SlabFactor(self.sys, seeds)
+            self._slab = SlabFactor(self.sys, seeds, locality_key(self.field, self.solve_ids))
             self._slab_key = None
         return self._slab
 

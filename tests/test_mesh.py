@@ -91,3 +91,21 @@ def test_iris_filter_keeps_only_apertures_in_iris_slabs():
         assert sel.any()
         assert np.all(c[0, sel] > (a - w) / 2) and np.all(c[0, sel] < (a + w) / 2)
         y += 2e-3 + ([15.8e-3, 17.6e-3, 18.0e-3, 17.6e-3, 15.8e-3] + [0.0])[i]
+
+
+def test_locality_key_pairs_entity_dofs():
+    """The slab order key is a permutation and puts the two DOFs of every kept edge
+    or face next to each other."""
+    from emerge_gb300.bc import PEC
+    from emerge_gb300.freq import Assembler
+    from emerge_gb300.mesh import FACE_XMIN, FACE_ZMAX, Nedelec2Basis, unit_cube
+    from emerge_gb300.solver import locality_key
+    field = Nedelec2Basis(unit_cube(3, jitter=0.1, seed=2))
+    sid = Assembler(device="cpu").solve_ids(field, [PEC([FACE_XMIN, FACE_ZMAX])])
+    key = locality_key(field, sid)
+    assert np.array_equal(np.sort(key), np.arange(sid.size))
+    nE, nF = field.mesh.edges.shape[1], field.mesh.tris.shape[1]
+    pos = {int(g): i for i, g in enumerate(sid)}
+    for g, i in pos.items():
+        if g < nE + nF and g + nE + nF in pos:
+            assert key[pos[g + nE + nF]] == key[i] + 1
