@@ -1,22 +1,25 @@
-"""Assembly benchmark: second-order Nédélec E/B assembly of the 80³ Kuhn unit cube.
+"""Benchmarks of the frequency-domain FEM hot path on one GPU; prints one JSON line.
 
-Workload (the reference's assembly micro-benchmark): unit cube, 80³ hexes × 6
-Kuhn tets (3,072,000 tets), interior vertices jittered by U[-0.15h, 0.15h]
-(numpy default_rng(0)); per tet εr ~ U[1,10], tanδ ~ U[0.001,0.02]
-(default_rng(1)), μr = 1.  One step = assembling the complex128 curl-curl (E)
-and mass (B) CSR matrices, i.e. tet_mass_stiffness_matrices
-(fem/physics/edm/optimized_assembly.py:43-64).  The CSR pattern is built once
-per mesh before timing (reported separately as ``plan_s``).
+Assembly (the line's metric/value; the reference's assembly micro-benchmark): unit
+cube, 80³ hexes × 6 Kuhn tets (3,072,000 tets), interior vertices jittered by
+U[-0.15h, 0.15h] (numpy default_rng(0)); per tet εr ~ U[1,10], tanδ ~ U[0.001,0.02]
+(default_rng(1)), μr = 1.  One step = assembling the complex128 curl-curl (E) and
+mass (B) CSR matrices, i.e. tet_mass_stiffness_matrices
+(fem/physics/edm/optimized_assembly.py:43-64).  The CSR pattern is built once per
+mesh before timing (reported separately as ``plan_s``).  ``value``: tets/s with
+inputs resident in HBM (each step writes 27.5 GB of values, far more than the 129 MB
+L2, so no L2 flush is needed).  ``e2e``: the same through the C-ABI host entry point
+(emg_assemble_tet_host), with the material H2D and the E/B D2H inside the timed
+region.  ``--impl reference`` times the reference's CPU algorithm (the oracle's C++
+restatement of the Numba element loop on all host cores + SciPy
+coo_matrix(...).tocsr()) on a bounded sample of the same workload.
+
+Sweep (``sweep``): the five-cavity iris filter, 401 points over 8-12 GHz x 2 ports,
+the batched mixed-precision warm-started GPU sweep against the plain FP64 GPU solver
+(see run_sweep).  Eigen (``eigen``): cavity eigenmodes (see run_eigen).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--n 80] [--impl reference]
-
-Prints one JSON line.  ``value``: tets/s with inputs resident in HBM (each step
-writes 27.5 GB of values, far more than the 129 MB L2, so no L2 flush is
-needed).  ``e2e``: the same through the C-ABI host entry point
-(emg_assemble_tet_host), with the material H2D and the E/B D2H inside the timed
-region.  ``--impl reference`` times the reference's CPU algorithm (the oracle's
-C++ restatement of the Numba element loop on all host cores + SciPy
-coo_matrix(...).tocsr()) on a bounded sample of the same workload.
+                  [--no-sweep] [--sweep-h 2e-3] [--eigen 2] [--sweep-only] [--eigen-only]
 """
 from __future__ import annotations
 
@@ -306,10 +309,14 @@ def run_sweep(args):
     nf = args.sweep_points
     freqs = np.linspace(8e9, 12e9, nf)
     idx = np.unique(np.linspace(0, nf - 1, args.sweep_plain + 2).astype(int)[1:-1])
-    chunk = args.sweep_chunk or None
+    # points per batched solve: every column at once unless the Krylov basis (V and Z,
+    # restart+1 and restart vectors of n x 2 columns per point, complex128) and the
+    # stored A(k) would pass ~80 GB
+    per_point = 16 * (2 * sw.sys.n * (2 * args.sweep_restart + 3) + sw.sys.nnz)
+    chunk = args.sweep_chunk or max(1, min(nf, int(80e9 // per_point)))
     out = {"workload": f"{p.name}: N={p.field.n_field} DOFs ({sw.sys.n} after PEC), {nf} points 8-12 GHz x 2 ports",
            "metric": "sweep freq-pts/s", "tol": args.sweep_tol, "setup_s": round(setup, 2),
-           "slabs": sl.info()["slabs"], "max_slab_width": sl.info()["max_width"]}
+           "slabs": sl.info()["slabs"], "max_slab_width": sl.info()["max_width"], "chunk_points": chunk}
     with ClockSampler(0) as clk:
         # warm-up of every code path on a tiny sweep (graph capture, cuBLAS/cuSOLVER handles)
         sw.run_warm(freqs[:4], n_train=2, solver="anchored", n_anchor=1, precision="fp32", guess="mlp",
@@ -451,16 +458,16 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=200_000, help="tets in the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the frequency-sweep measurement")
-    ap.add_argument("--sweep-h", type=float, default=3e-3, help="iris-filter mesh size (m)")
+    ap.add_argument("--sweep-h", type=float, default=2e-3, help="iris-filter mesh size (m)")
     ap.add_argument("--sweep-points", type=int, default=401)
     ap.add_argument("--sweep-train", type=int, default=32)
     ap.add_argument("--sweep-anchors", type=int, default=8)
     ap.add_argument("--sweep-restart", type=int, default=40)
-    ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: all)")
+    ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: as many as fit ~80 GB)")
     ap.add_argument("--sweep-mlp-steps", type=int, default=1500)
     ap.add_argument("--sweep-inner", default="fp64", choices=["fp32", "fp64"],
                     help="precision of the Krylov vectors of the fast sweep (its factors are FP32 either way)")
-    ap.add_argument("--sweep-refine", type=int, default=1, help="Newton-Schulz step on the FP32 slab inverses")
+    ap.add_argument("--sweep-refine", type=int, default=0, help="Newton-Schulz step on the FP32 slab inverses")
     ap.add_argument("--sweep-plain", type=int, default=2)
     ap.add_argument("--sweep-ilu-iters", type=int, default=1000)
     ap.add_argument("--sweep-cpu", type=int, default=1, help="points solved by SciPy SuperLU on the host")
