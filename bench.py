@@ -343,6 +343,9 @@ def run_sweep(args):
         "mlp_seconds": round(fast.info["guess_seconds"], 3), "mlp_loss": fast.info["mlp_loss"],
         "final_seconds": round(fast.info["final_seconds"], 3),
         "iterations_fast_mean": float(fast.iterations.mean()), "iterations_fast_max": int(fast.iterations.max()),
+        # iterations on the points the warm start predicts (all but the training points)
+        "iterations_warm_predicted_mean": fast.info["final_iterations_mean"],
+        "iterations_cold_same_points_mean": float(cold.iterations[fast.info["final_index"]].mean()),
         "iterations_cold_mean": float(cold.iterations.mean()), "cold_pts_per_s": nf / cold.seconds,
         "max_abs_dS_cold_vs_fast": float(np.max(np.abs(cold.S - fast.S))),
         "projection_pts_per_s": nf / proj.seconds, "iterations_projection_mean": float(proj.iterations.mean()),
@@ -464,7 +467,7 @@ def main():
     ap.add_argument("--sweep-anchors", type=int, default=8)
     ap.add_argument("--sweep-restart", type=int, default=40)
     ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: as many as fit ~80 GB)")
-    ap.add_argument("--sweep-mlp-steps", type=int, default=1500)
+    ap.add_argument("--sweep-mlp-steps", type=int, default=1000)
     ap.add_argument("--sweep-inner", default="fp64", choices=["fp32", "fp64"],
                     help="precision of the Krylov vectors of the fast sweep (its factors are FP32 either way)")
     ap.add_argument("--sweep-refine", type=int, default=0, help="Newton-Schulz step on the FP32 slab inverses")

@@ -943,7 +943,8 @@ int gmres_run(emg_rplan* p, int64_t Bc, const MatArg& A, const double2* rhs, dou
     };
     kry::k_sqrt_real<<<cgrid, 128, 0, s>>>(Bc, norms2(rhs), bn);
     EMG_CUDA(cudaMemsetAsync(its, 0, sizeof(int32_t) * Bc, s));
-    // one Arnoldi step for Krylov index j (captured once per j into a CUDA graph)
+    // one Arnoldi step for Krylov index j (from the first restart on, captured once
+    // per j into a CUDA graph)
     auto step = [&](int j) -> int {
         double2* Vj = V + (int64_t)j * vec;
         double2* Mv = flexible ? Z + (int64_t)j * vec : Tv;
@@ -973,7 +974,7 @@ int gmres_run(emg_rplan* p, int64_t Bc, const MatArg& A, const double2* rhs, dou
     } guard{&graphs};
     int total = 0;
     std::vector<int32_t> hact(Bc), hprev(Bc), hits(Bc, 0);
-    while (total < max_iter) {
+    for (int cycle = 0; total < max_iter; ++cycle) {
         // r = b - A x ; V0 = r / ||r||
         spmv_op(p, Bc, A, x, rhs, W, s);
         double2* rr = norms2(W);
@@ -987,19 +988,26 @@ int gmres_run(emg_rplan* p, int64_t Bc, const MatArg& A, const double2* rhs, dou
         if (!any) break;
         int j = 0;
         while (j < m && total < max_iter) {
-            if (!graphs[j]) {
-                cudaGraph_t gr = nullptr;
-                EMG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                const int rc = step(j);
-                const cudaError_t ec = cudaStreamEndCapture(s, &gr);
-                if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
-                if (ec != cudaSuccess) return cuda_status(ec, "cudaStreamEndCapture");
-                const cudaError_t ei = cudaGraphInstantiate(&graphs[j], gr, 0);
-                cudaGraphDestroy(gr);
-                if (ei != cudaSuccess) return cuda_status(ei, "cudaGraphInstantiate");
-            }
             hprev = hact;
-            EMG_CUDA(cudaGraphLaunch(graphs[j], s));
+            if (cycle == 0) {
+                // first cycle: direct launches (a graph would be instantiated for one use)
+                const int rc = step(j);
+                if (rc) return rc;
+            } else {
+                // restarted cycles replay each Arnoldi step's graph
+                if (!graphs[j]) {
+                    cudaGraph_t gr = nullptr;
+                    EMG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                    const int rc = step(j);
+                    const cudaError_t ec = cudaStreamEndCapture(s, &gr);
+                    if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+                    if (ec != cudaSuccess) return cuda_status(ec, "cudaStreamEndCapture");
+                    const cudaError_t ei = cudaGraphInstantiate(&graphs[j], gr, 0);
+                    cudaGraphDestroy(gr);
+                    if (ei != cudaSuccess) return cuda_status(ei, "cudaGraphInstantiate");
+                }
+                EMG_CUDA(cudaGraphLaunch(graphs[j], s));
+            }
             ++j;
             ++total;
             EMG_CUDA(cudaMemcpyAsync(hact.data(), act, sizeof(int32_t) * Bc, cudaMemcpyDeviceToHost, s));
@@ -1076,6 +1084,7 @@ struct Inner32 {
             *y = nullptr;
     double *bn = nullptr, *vs = nullptr, *wn = nullptr, *res = nullptr;
     int32_t *act = nullptr, *len = nullptr;
+    int cycles = 0;                      // Arnoldi cycles run so far (graphs from the second on)
     std::vector<cudaGraphExec_t> graphs;
     ~Inner32() {
         for (auto& e : graphs)
@@ -1134,19 +1143,24 @@ int gmres32(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const flo
         if (!any) break;
         int j = 0;
         while (j < m && total < max_iter) {
-            if (!w.graphs[j]) {
-                cudaGraph_t gr = nullptr;
-                EMG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                const int rc = step(j);
-                const cudaError_t ec = cudaStreamEndCapture(s, &gr);
-                if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
-                if (ec != cudaSuccess) return cuda_status(ec, "cudaStreamEndCapture");
-                const cudaError_t ei = cudaGraphInstantiate(&w.graphs[j], gr, 0);
-                cudaGraphDestroy(gr);
-                if (ei != cudaSuccess) return cuda_status(ei, "cudaGraphInstantiate");
-            }
             hprev = hact;
-            EMG_CUDA(cudaGraphLaunch(w.graphs[j], s));
+            if (w.cycles == 0) {
+                const int rc = step(j);
+                if (rc) return rc;
+            } else {
+                if (!w.graphs[j]) {
+                    cudaGraph_t gr = nullptr;
+                    EMG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                    const int rc = step(j);
+                    const cudaError_t ec = cudaStreamEndCapture(s, &gr);
+                    if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+                    if (ec != cudaSuccess) return cuda_status(ec, "cudaStreamEndCapture");
+                    const cudaError_t ei = cudaGraphInstantiate(&w.graphs[j], gr, 0);
+                    cudaGraphDestroy(gr);
+                    if (ei != cudaSuccess) return cuda_status(ei, "cudaGraphInstantiate");
+                }
+                EMG_CUDA(cudaGraphLaunch(w.graphs[j], s));
+            }
             ++j;
             ++total;
             EMG_CUDA(cudaMemcpyAsync(hact.data(), w.act, sizeof(int32_t) * Bc, cudaMemcpyDeviceToHost, s));
@@ -1161,6 +1175,7 @@ int gmres32(emg_rplan* p, int64_t Bc, const int32_t* cmat, int64_t Bm, const flo
         kry::k_backsolve<<<cgrid, 128, 0, s>>>(Bc, m, w.H, w.g, w.len, w.y, j);
         kry::k_combine32<<<grid_for(vec, T), T, 0, s>>>(n, Bc, j, w.Z, vec, w.y, x);
         EMG_CUDA(cudaGetLastError());
+        ++w.cycles;
     }
     return EMG_OK;
 }

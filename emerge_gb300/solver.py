@@ -695,6 +695,21 @@ class FrequencySweep:
         yc = torch.complex(P[:, :r], P[:, r:])
         return (Q @ yc.T).contiguous(), hist[-1]
 
+    def _merge(self, freqs, idx_a, res_a: SweepResult, idx_b, res_b: SweepResult) -> SweepResult:
+        """One SweepResult over ``freqs`` from results on the index sets idx_a and idx_b."""
+        nf, npo = len(freqs), len(self.ports)
+        X = torch.empty((self.sys.n, nf, npo), dtype=torch.complex128, device=self.device)
+        X[:, idx_a] = res_a.solutions.reshape(self.sys.n, len(idx_a), npo)
+        X[:, idx_b] = res_b.solutions.reshape(self.sys.n, len(idx_b), npo)
+        S = np.empty((nf, npo, npo), dtype=np.complex128)
+        S[idx_a], S[idx_b] = res_a.S, res_b.S
+        its = np.empty((nf, npo), dtype=np.int64)
+        its[idx_a], its[idx_b] = res_a.iterations, res_b.iterations
+        rs = np.empty((nf, npo))
+        rs[idx_a], rs[idx_b] = res_a.residuals, res_b.residuals
+        return SweepResult(freqs, S, its, rs, res_a.seconds + res_b.seconds, X.reshape(self.sys.n, nf * npo),
+                           dict(res_b.info))
+
     def run_warm(self, freqs, n_train: int = 32, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
                  chunk: int | None = None, guess: str = "projection", solver: str = "ilu0", n_anchor: int = 4,
                  precision: str = "fp32", mlp_steps: int = 1500, refine: int = 0, inner: str = "fp64") -> SweepResult:
@@ -728,12 +743,18 @@ class FrequencySweep:
             X0 = None
         torch.cuda.synchronize()
         t_guess = time.perf_counter() - tg
-        rest = solve(freqs, X0)
+        # the training points are done: solve the others and keep their solutions
+        others = np.setdiff1d(np.arange(nf), tr)
+        x0_others = None if X0 is None else X0.reshape(-1, nf, npo)[:, others].reshape(X0.shape[0], -1)
+        rest_part = solve(freqs[others], x0_others)
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
-        info = {"train_points": len(tr), "train_iterations": first.iterations, "train_seconds": first.seconds,
-                "guess_seconds": t_guess, "final_seconds": rest.seconds, "guess": guess, "mlp_loss": mlp_loss,
-                "solver": solver, **({k: v for k, v in first.info.items()} if solver == "anchored" else {})}
+        rest = self._merge(freqs, tr, first, others, rest_part)
+        info = {"train_points": len(tr), "train_index": tr, "train_iterations": first.iterations,
+                "train_seconds": first.seconds, "guess_seconds": t_guess, "final_seconds": rest_part.seconds,
+                "final_index": others, "final_iterations_mean": float(rest_part.iterations.mean()) if others.size else 0.0,
+                "guess": guess, "mlp_loss": mlp_loss, "solver": solver,
+                **({k: v for k, v in first.info.items()} if solver == "anchored" else {})}
         return SweepResult(freqs, rest.S, rest.iterations, rest.residuals, secs, rest.solutions, info)
 
 
