@@ -63,6 +63,14 @@ void spmv_op(const emg_rplan* p, int64_t Bc, const MatArg& A, const double2* X, 
 int gmres_run(emg_rplan* p, int64_t Bc, const MatArg& A, const double2* rhs, double2* x, int restart, int max_iter,
               double tol, int32_t* iters_out, double* resid_out, cudaStream_t caller, Precond& M, bool flexible);
 
+// Complex slab product on the tcgen05 tensor cores (TF32 products, FP32 accumulation;
+// emg_tc.cu): Out[row0 + r, cols of group] = alpha S_g[r, :] Y[row0 + :, cols] + beta
+// Out for the 16-byte group records {factor, col0, ncol, pad}; status (device) set
+// to 1 if a bounded wait ran out.
+int tc_slab_product(int64_t w, int64_t row0, int64_t Bc, const void* groups, int G, int maxcol, const float2* Sinv,
+                    int64_t totD, int64_t offD, const float2* Y, float alpha, int beta, float2* Out, int32_t* status,
+                    cudaStream_t st);
+
 // Preconditioner on FP32 vectors (the inner solves of the mixed-precision refinement).
 struct Precond32 {
     virtual ~Precond32() = default;

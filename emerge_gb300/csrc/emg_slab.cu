@@ -595,27 +595,66 @@ __global__ void __launch_bounds__(kThreads) k_rowmv(int64_t w, int64_t row0, int
     }
 }
 
-// The same product for wide groups: 64 x 64 output tiles through tile_mac.
-// Grid: column tiles x row tiles x groups.
+// The same product for wide groups: 64 x 64 output tiles through tile_mac, with
+// the K range split over ``splits`` CTAs when the tiles alone would not fill the
+// GPU.  A split writes its partial tile to ``part``; the last split of a tile to
+// arrive (per-tile counter) adds the partials in split order, so the result does
+// not depend on arrival order, writes the output and resets the counter.
+// Grid: column tiles x (row tiles * splits) x groups.
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_slab_gemm(int64_t w, int64_t row0, int64_t Bc,
                                                         const Group* __restrict__ groups,
                                                         const typename C2<R>::T* __restrict__ Sinv, int64_t totD,
                                                         int64_t offD, const typename C2<R>::T* __restrict__ Y, R alpha,
-                                                        int beta, typename C2<R>::T* __restrict__ Out) {
+                                                        int beta, typename C2<R>::T* __restrict__ Out, int splits,
+                                                        typename C2<R>::T* __restrict__ part, int32_t* __restrict__ cnt) {
     using T = typename C2<R>::T;
     __shared__ Tile<R> sm;
+    __shared__ int s_last;
     const Group g = groups[blockIdx.z];
-    const int64_t c0 = (int64_t)blockIdx.x * kTile, r0 = (int64_t)blockIdx.y * kTile;
+    const int rt = (int)blockIdx.y / splits, sp = (int)blockIdx.y % splits;
+    const int64_t c0 = (int64_t)blockIdx.x * kTile, r0 = (int64_t)rt * kTile;
     if (c0 >= g.ncol) return;
     const int nr = (int)min((int64_t)kTile, w - r0), nc = (int)min((int64_t)kTile, (int64_t)g.ncol - c0);
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    const int64_t kper = (w + splits - 1) / splits;
+    const int64_t ks0 = min(w, (int64_t)sp * kper), ks1 = min(w, ks0 + kper);
     T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
-    tile_mac<R>(acc, Sinv + (int64_t)g.fac * totD + offD + r0 * w, w, Y + row0 * Bc + g.col0 + c0, Bc, nr, nc, w, sm);
+    tile_mac<R>(acc, Sinv + (int64_t)g.fac * totD + offD + r0 * w + ks0, w, Y + (row0 + ks0) * Bc + g.col0 + c0, Bc, nr,
+                nc, ks1 - ks0, sm);
+    if (splits > 1) {
+        const int64_t tile = ((int64_t)blockIdx.z * (gridDim.y / splits) + rt) * gridDim.x + blockIdx.x;
+        T* mine = part + (tile * splits + sp) * (kTile * kTile);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) mine[(ty + 16 * i) * kTile + tx + 16 * j] = acc[i][j];
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) s_last = atomicAdd(cnt + tile, 1) == splits - 1;
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        const T* all = part + tile * splits * (kTile * kTile);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int e = (ty + 16 * i) * kTile + tx + 16 * j;
+                T v = czero<T>();
+                for (int q = 0; q < splits; ++q) {
+                    const T pq = __ldcg(all + (int64_t)q * kTile * kTile + e);
+                    v.x += pq.x;
+                    v.y += pq.y;
+                }
+                acc[i][j] = v;
+            }
+        if (tid == 0) cnt[tile] = 0;
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -628,6 +667,14 @@ __global__ void __launch_bounds__(kThreads) k_slab_gemm(int64_t w, int64_t row0,
                 else o = res;
             }
         }
+}
+
+// K splits of a wide-group product: enough CTAs for two per SM, at least 256
+// columns of K per split, at most 8.
+inline int gemm_splits(int64_t tiles, int64_t w) {
+    int64_t sp = (2 * 152 + tiles - 1) / std::max<int64_t>(tiles, 1);
+    sp = std::min<int64_t>(sp, std::max<int64_t>(1, w / 256));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(sp, 8));
 }
 
 }  // namespace slab
@@ -661,6 +708,12 @@ struct emg_slab {
     int32_t* colfac = nullptr;
     emg::slab::Group* groups = nullptr;
     int64_t ngroups_cap = 0;
+    void* kpart = nullptr;            // split-K partial tiles of the wide-group products
+    size_t kpart_bytes = 0;
+    int32_t* kcnt = nullptr;          // per-tile arrival counters (zero between launches)
+    int64_t kcnt_n = 0;
+    int use_tc = 0;                   // wide-group products of FP32 factors on the tcgen05 tensor cores
+    int32_t* tc_status = nullptr;     // set by a tensor-core tile whose bounded wait ran out
 };
 
 namespace {
@@ -677,7 +730,8 @@ void slab_free(emg_slab* s) {
     slab_free_factors(s);
     dfree(s->perm); dfree(s->dmap); dfree(s->cptr); dfree(s->csrc); dfree(s->cidx); dfree(s->uptr); dfree(s->usrc);
     dfree(s->uidx); dfree(s->ucptr); dfree(s->ucsrc); dfree(s->ucrow); dfree(s->Y); dfree(s->Z); dfree(s->colfac);
-    dfree(s->groups);
+    dfree(s->groups); dfree(s->tc_status); dfree(s->kcnt);
+    if (s->kpart) cudaFree(s->kpart);
     delete s;
 }
 
@@ -1001,6 +1055,20 @@ extern "C" int emg_slab_factor(emg_slab* s, int precision, int64_t F, const int3
 }
 
 namespace {
+// EMG_ERR_CUDA if a tensor-core tile of the last solve gave up waiting (and reset).
+int tc_check(emg_slab* s, cudaStream_t st) {
+    if (!s->tc_status || !s->use_tc) return EMG_OK;
+    int32_t h = 0;
+    EMG_CUDA(cudaMemcpyAsync(&h, s->tc_status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    EMG_CUDA(cudaStreamSynchronize(st));
+    if (h) {
+        EMG_CUDA(cudaMemset(s->tc_status, 0, sizeof(int32_t)));
+        set_error("slab solve: a tensor-core tile timed out waiting for its MMAs");
+        return EMG_ERR_CUDA;
+    }
+    return EMG_OK;
+}
+
 // The slab solve as a GMRES preconditioner: column c uses factor cfac[c].
 struct SlabPrecond : emg::Precond {
     emg_slab* s;
@@ -1029,6 +1097,43 @@ struct SlabPrecond : emg::Precond {
             s->ws_cols = bc;
             s->ws_bytes = bytes;
         }
+        // split-K scratch for the wide-group products (largest need over the slabs)
+        int maxcol = 0;
+        for (const auto& g : groups) maxcol = std::max(maxcol, (int)g.ncol);
+        if (maxcol >= emg::slab::kWideGroup) {
+            const int64_t ct = (maxcol + emg::slab::kTile - 1) / emg::slab::kTile, G = (int64_t)groups.size();
+            size_t need = 0;
+            int64_t tiles_max = 0;
+            for (int i = 0; i < s->m; ++i) {
+                const int64_t w = s->off[i + 1] - s->off[i];
+                const int64_t tiles = ct * ((w + emg::slab::kTile - 1) / emg::slab::kTile) * G;
+                const int sp = emg::slab::gemm_splits(tiles, w);
+                tiles_max = std::max(tiles_max, tiles);
+                if (sp > 1)
+                    need = std::max(need, (size_t)tiles * sp * emg::slab::kTile * emg::slab::kTile *
+                                              (s->prec == 1 ? sizeof(float2) : sizeof(double2)));
+            }
+            if (need > s->kpart_bytes) {
+                if (s->kpart) cudaFree(s->kpart);
+                s->kpart = nullptr;
+                s->kpart_bytes = 0;
+                EMG_CUDA(cudaMalloc(&s->kpart, need));
+                s->kpart_bytes = need;
+            }
+            if (tiles_max > s->kcnt_n) {
+                dfree(s->kcnt);
+                s->kcnt_n = 0;
+                int rc = dalloc(&s->kcnt, tiles_max, "slab split-K counters");
+                if (rc) return rc;
+                EMG_CUDA(cudaMemset(s->kcnt, 0, sizeof(int32_t) * tiles_max));
+                s->kcnt_n = tiles_max;
+            }
+        }
+        if (!s->tc_status) {
+            int rc = dalloc(&s->tc_status, 1, "slab tensor-core status");
+            if (rc) return rc;
+            EMG_CUDA(cudaMemset(s->tc_status, 0, sizeof(int32_t)));
+        }
         if ((int64_t)groups.size() > s->ngroups_cap) {
             dfree(s->groups);
             int rc = dalloc(&s->groups, (int64_t)groups.size(), "slab groups");
@@ -1053,11 +1158,22 @@ struct SlabPrecond : emg::Precond {
         for (const auto& g : groups) maxcol = std::max(maxcol, (int)g.ncol);
         // dense slab product: warp-per-row for narrow groups, 64 x 64 tiles for wide ones
         auto dense = [&](int64_t w, int64_t i, R alpha, int beta) {
-            if (maxcol >= kWideGroup)
-                k_slab_gemm<R><<<dim3((unsigned)((maxcol + kTile - 1) / kTile), (unsigned)((w + kTile - 1) / kTile), G),
-                                 kThreads, 0, st>>>(w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, alpha,
-                                                    beta, Z);
-            else
+            if constexpr (sizeof(R) == 4) {
+                if (s->use_tc && maxcol >= kWideGroup) {
+                    emg::tc_slab_product(w, s->off[i], Bc, s->groups, (int)G, maxcol,
+                                         reinterpret_cast<const float2*>(Sinv), s->totD, s->offD[i],
+                                         reinterpret_cast<const float2*>(Y), (float)alpha, beta,
+                                         reinterpret_cast<float2*>(Z), s->tc_status, st);
+                    return;
+                }
+            }
+            if (maxcol >= kWideGroup) {
+                const int64_t ct = (maxcol + kTile - 1) / kTile, rt = (w + kTile - 1) / kTile;
+                const int sp = gemm_splits(ct * rt * G, w);
+                k_slab_gemm<R><<<dim3((unsigned)ct, (unsigned)(rt * sp), G), kThreads, 0, st>>>(
+                    w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, alpha, beta, Z, sp,
+                    static_cast<T*>(s->kpart), s->kcnt);
+            } else
                 k_rowmv<R><<<dim3((unsigned)((w * 32 + kThreads - 1) / kThreads), G), kThreads, 0, st>>>(
                     w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, alpha, beta, Z);
         };
@@ -1104,7 +1220,9 @@ extern "C" int emg_slab_apply(emg_slab* s, int64_t Bc, const int32_t* cfac, cons
     SlabPrecond M(s, Bc, cfac);
     int rc = M.prepare(Bc);
     if (rc) return rc;
-    return M.apply(reinterpret_cast<const double2*>(X_in), reinterpret_cast<double2*>(X_out), (cudaStream_t)stream);
+    rc = M.apply(reinterpret_cast<const double2*>(X_in), reinterpret_cast<double2*>(X_out), (cudaStream_t)stream);
+    if (rc) return rc;
+    return tc_check(s, (cudaStream_t)stream);
 }
 
 extern "C" int emg_gmres_slab(const emg_rplan* pc, emg_slab* s, int64_t Bc, const int32_t* cmat, int64_t Bm,
@@ -1122,8 +1240,15 @@ extern "C" int emg_gmres_slab(const emg_rplan* pc, emg_slab* s, int64_t Bc, cons
     Am.A = reinterpret_cast<const double2*>(A);
     Am.Bm = Bm;
     Am.cmat = cmat;
-    return gmres_run(p, Bc, Am, reinterpret_cast<const double2*>(rhs), reinterpret_cast<double2*>(x), restart, max_iter,
-                     tol, iters_out, resid_out, (cudaStream_t)stream, M, true);
+    const int rc = gmres_run(p, Bc, Am, reinterpret_cast<const double2*>(rhs), reinterpret_cast<double2*>(x), restart,
+                             max_iter, tol, iters_out, resid_out, (cudaStream_t)stream, M, true);
+    return rc ? rc : tc_check(s, (cudaStream_t)stream);
+}
+
+extern "C" int emg_slab_set_tensor_cores(emg_slab* s, int on) {
+    EMG_CHECK_ARG(s, "emg_slab_set_tensor_cores: NULL argument");
+    s->use_tc = on ? 1 : 0;
+    return EMG_OK;
 }
 
 extern "C" int emg_gmres_slab_family(const emg_rplan* pc, emg_slab* s, int64_t Bc, int nfam, const double* fam,

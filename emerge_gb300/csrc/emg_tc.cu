@@ -1,0 +1,366 @@
+// 5th-generation tensor-core (tcgen05) TF32 GEMM tile for the dense slab products.
+//
+// D[M x N] = A[M x K] B[N x K]^T (row-major FP32 in and out, TF32 products, FP32
+// accumulation in tensor memory).  One CTA of 128 threads owns a 128 x 64 tile of D:
+//   - the operands of a 32-wide K chunk are staged by all threads into shared memory
+//     in the canonical K-major, non-swizzled layout (8-row x 16-byte core matrices,
+//     K-adjacent core matrices 128 B apart, M/N-adjacent 1024 / 1024 B apart);
+//   - one elected thread issues four tcgen05.mma (K = 8 each) per chunk and commits
+//     them to an mbarrier; every thread waits on it (bounded) before the next chunk
+//     overwrites the staging buffers;
+//   - the accumulator (128 lanes x 64 columns of TMEM) is read back with
+//     tcgen05.ld.32x32b (warp w reads lanes 32w..32w+31) and stored.
+// Every wait is bounded: on timeout the CTA records an error in *status, skips the
+// remaining work, and still frees its TMEM.
+#include "emg_krylov.cuh"
+
+namespace emg {
+namespace tc {
+
+constexpr int kM = 128, kN = 64, kK = 32, kThreads = 128;
+constexpr uint32_t kTmemCols = 64;
+constexpr long long kSpinLimit = 1ll << 16;   // a chunk's MMAs finish in well under a microsecond
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// UMMA shared-memory descriptor, K-major, no swizzle: start address, leading
+// (K-direction) byte offset, stride (M/N-direction) byte offset, all >> 4; bits
+// 46-47 = 0b01 (descriptor version).
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32 (format 2
+// in bits 7-9 and 10-12), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    for (long long it = 0; it < kSpinLimit; ++it) {
+        uint32_t done = 0;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// byte offset of element (r, k) of a [rows x 32] K-major tile in the canonical layout
+__device__ __forceinline__ uint32_t tile_off(int r, int k) {
+    return (uint32_t)(((r >> 3) * (kK / 4) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+
+__global__ void __launch_bounds__(kThreads) k_gemm_tf32(int64_t M, int64_t N, int64_t K, const float* __restrict__ A,
+                                                        int64_t lda, const float* __restrict__ B, int64_t ldb,
+                                                        float* __restrict__ D, int64_t ldd, int32_t* __restrict__ status) {
+    __shared__ __align__(1024) float sa[kM * kK];
+    __shared__ __align__(1024) float sb[kN * kK];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t m0 = (int64_t)blockIdx.y * kM, n0 = (int64_t)blockIdx.x * kN;
+    if (tid == 0) {
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = tmem_base;
+    const uint32_t mb = smem_u32(&mbar);
+    uint32_t phase = 0;
+    const int64_t nk = (K + kK - 1) / kK;
+    for (int64_t kc = 0; kc < nk; ++kc) {
+        const int64_t k0 = kc * kK;
+        // stage A (128 x 32) and B (64 x 32), zero outside the matrices
+        for (int idx = tid; idx < kM * kK; idx += kThreads) {
+            const int r = idx / kK, k = idx % kK;
+            const int64_t gr = m0 + r, gk = k0 + k;
+            const float v = (gr < M && gk < K) ? A[gr * lda + gk] : 0.f;
+            *reinterpret_cast<float*>(reinterpret_cast<char*>(sa) + tile_off(r, k)) = v;
+        }
+        for (int idx = tid; idx < kN * kK; idx += kThreads) {
+            const int r = idx / kK, k = idx % kK;
+            const int64_t gr = n0 + r, gk = k0 + k;
+            const float v = (gr < N && gk < K) ? B[gr * ldb + gk] : 0.f;
+            *reinterpret_cast<float*>(reinterpret_cast<char*>(sb) + tile_off(r, k)) = v;
+        }
+        // make the generic-proxy stores visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0 && !s_fail) {
+            const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+            const uint32_t idesc = idesc_tf32(kM, kN);
+#pragma unroll
+            for (int ks = 0; ks < kK / 8; ++ks) {
+                // K = 8 TF32 = two core matrices along K: +256 B per step
+                const uint64_t ad = make_desc(a0 + ks * 256, 128, 1024);
+                const uint64_t bd = make_desc(b0 + ks * 256, 128, 1024);
+                const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(taddr),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                         : "memory");
+        }
+        __syncthreads();
+        if (!s_fail) {
+            if (!mbar_wait(mb, phase)) s_fail = 1;
+        }
+        phase ^= 1;
+        __syncthreads();
+        if (s_fail) break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!s_fail) {
+        // warp w reads TMEM lanes 32w..32w+31 (rows of the tile), 64 columns
+        uint32_t v[kN];
+        const uint32_t lane_addr = taddr + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < kN; c0 += 16) {
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(v[c0 + 0]), "=r"(v[c0 + 1]), "=r"(v[c0 + 2]), "=r"(v[c0 + 3]), "=r"(v[c0 + 4]), "=r"(v[c0 + 5]),
+                  "=r"(v[c0 + 6]), "=r"(v[c0 + 7]), "=r"(v[c0 + 8]), "=r"(v[c0 + 9]), "=r"(v[c0 + 10]),
+                  "=r"(v[c0 + 11]), "=r"(v[c0 + 12]), "=r"(v[c0 + 13]), "=r"(v[c0 + 14]), "=r"(v[c0 + 15])
+                : "r"(lane_addr + (uint32_t)c0)
+                : "memory");
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const int64_t row = m0 + warp * 32 + lane;
+        if (row < M) {
+#pragma unroll
+            for (int c = 0; c < kN; ++c)
+                if (n0 + c < N) D[row * ldd + n0 + c] = __uint_as_float(v[c]);
+        }
+    } else {
+        // timed out: give the committed MMAs one more bounded wait before the TMEM goes
+        if (tid == 0) {
+            mbar_wait(mb, phase ^ 1);
+            atomicExch(status, 1);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kTmemCols) : "memory");
+}
+
+// Complex product of the slab solve on the tensor cores: Out[r0.., cols] =
+// alpha * S[128 rows x K] Y[K x 64 cols] + beta * Out, complex64 interleaved in and
+// out, TF32 products.  Real and imaginary parts of both operands are staged as four
+// K-major tiles; per K step of 8 the real accumulator (TMEM columns 0-63) takes
+// Sre Yre and -Sim Yim (negation in the instruction descriptor), the imaginary one
+// (columns 64-127) Sre Yim and Sim Yre.  Grid: column tiles x row tiles x groups;
+// each group g has its own S (factor) and column range (see emg_slab.cu).
+struct TcGroup {
+    int32_t fac, col0, ncol, pad;
+};
+constexpr int kCxSmem = 2 * kM * kK * 4 + 2 * kN * kK * 4;   // Sre, Sim, Yre, Yim tiles: 48 KB
+
+__global__ void __launch_bounds__(kThreads) k_cgemm_tf32(int64_t w, int64_t row0, int64_t Bc,
+                                                         const TcGroup* __restrict__ groups,
+                                                         const float2* __restrict__ Sinv, int64_t totD, int64_t offD,
+                                                         const float2* __restrict__ Y, float alpha, int beta,
+                                                         float2* __restrict__ Out, int32_t* __restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char dsm[];
+    char* sar = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(dsm) + 1023) & ~(uintptr_t)1023);
+    char* sai = sar + kM * kK * 4;
+    char* sbr = sai + kM * kK * 4;
+    char* sbi = sbr + kN * kK * 4;
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_fail;
+    const TcGroup g = groups[blockIdx.z];
+    const int64_t c0 = (int64_t)blockIdx.x * kN, r0 = (int64_t)blockIdx.y * kM;
+    if (c0 >= g.ncol) return;          // uniform per CTA, before any TMEM allocation
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const float2* S = Sinv + (int64_t)g.fac * totD + offD;
+    const float2* Yb = Y + row0 * Bc + g.col0 + c0;
+    const int ncl = (int)min((int64_t)kN, (int64_t)g.ncol - c0);
+    if (tid == 0) {
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(2 * kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = tmem_base;
+    const uint32_t mb = smem_u32(&mbar);
+    uint32_t phase = 0;
+    const int64_t nk = (w + kK - 1) / kK;
+    for (int64_t kc = 0; kc < nk; ++kc) {
+        const int64_t k0 = kc * kK;
+        for (int idx = tid; idx < kM * kK; idx += kThreads) {
+            const int r = idx / kK, k = idx % kK;
+            const int64_t gr = r0 + r, gk = k0 + k;
+            const float2 v = (gr < w && gk < w) ? S[gr * w + gk] : make_float2(0.f, 0.f);
+            const uint32_t o = tile_off(r, k);
+            *reinterpret_cast<float*>(sar + o) = v.x;
+            *reinterpret_cast<float*>(sai + o) = v.y;
+        }
+        for (int idx = tid; idx < kN * kK; idx += kThreads) {
+            const int k = idx / kN, c = idx % kN;
+            const int64_t gk = k0 + k;
+            const float2 v = (c < ncl && gk < w) ? Yb[gk * Bc + c] : make_float2(0.f, 0.f);
+            const uint32_t o = tile_off(c, k);
+            *reinterpret_cast<float*>(sbr + o) = v.x;
+            *reinterpret_cast<float*>(sbi + o) = v.y;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0 && !s_fail) {
+            const uint32_t ar = smem_u32(sar), ai = smem_u32(sai), br = smem_u32(sbr), bi = smem_u32(sbi);
+            const uint32_t id = idesc_tf32(kM, kN), idneg = id | (1u << 13);
+            const uint32_t dre = taddr, dim = taddr + kTmemCols;
+#pragma unroll
+            for (int ks = 0; ks < kK / 8; ++ks) {
+                const uint32_t off = ks * 256;
+                const uint32_t first = (kc == 0 && ks == 0) ? 0u : 1u;
+                const uint64_t dar = make_desc(ar + off, 128, 1024), dai = make_desc(ai + off, 128, 1024);
+                const uint64_t dbr = make_desc(br + off, 128, 1024), dbi = make_desc(bi + off, 128, 1024);
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dre),
+                    "l"(dar), "l"(dbr), "r"(id), "r"(first)
+                    : "memory");
+                asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(dre), "l"(dai), "l"(dbi),
+                             "r"(idneg)
+                             : "memory");
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dim),
+                    "l"(dar), "l"(dbi), "r"(id), "r"(first)
+                    : "memory");
+                asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(dim), "l"(dai), "l"(dbr),
+                             "r"(id)
+                             : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                         : "memory");
+        }
+        __syncthreads();
+        if (!s_fail) {
+            if (!mbar_wait(mb, phase)) s_fail = 1;
+        }
+        phase ^= 1;
+        __syncthreads();
+        if (s_fail) break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!s_fail) {
+        const uint32_t lane_addr = taddr + ((uint32_t)(warp * 32) << 16);
+        const int64_t r = r0 + warp * 32 + lane;
+#pragma unroll
+        for (int cb = 0; cb < kN; cb += 16) {
+            uint32_t vr[16], vi[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(vr[0]), "=r"(vr[1]), "=r"(vr[2]), "=r"(vr[3]), "=r"(vr[4]), "=r"(vr[5]), "=r"(vr[6]),
+                  "=r"(vr[7]), "=r"(vr[8]), "=r"(vr[9]), "=r"(vr[10]), "=r"(vr[11]), "=r"(vr[12]), "=r"(vr[13]),
+                  "=r"(vr[14]), "=r"(vr[15])
+                : "r"(lane_addr + (uint32_t)cb)
+                : "memory");
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(vi[0]), "=r"(vi[1]), "=r"(vi[2]), "=r"(vi[3]), "=r"(vi[4]), "=r"(vi[5]), "=r"(vi[6]),
+                  "=r"(vi[7]), "=r"(vi[8]), "=r"(vi[9]), "=r"(vi[10]), "=r"(vi[11]), "=r"(vi[12]), "=r"(vi[13]),
+                  "=r"(vi[14]), "=r"(vi[15])
+                : "r"(lane_addr + kTmemCols + (uint32_t)cb)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (r < w) {
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    if (cb + c < ncl) {
+                        float2& o = Out[(row0 + r) * Bc + g.col0 + c0 + cb + c];
+                        const float2 res = make_float2(alpha * __uint_as_float(vr[c]), alpha * __uint_as_float(vi[c]));
+                        if (beta) { o.x += res.x; o.y += res.y; }
+                        else o = res;
+                    }
+                }
+            }
+        }
+    } else if (tid == 0) {
+        mbar_wait(mb, phase ^ 1);
+        atomicExch(status, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(2 * kTmemCols)
+                     : "memory");
+}
+
+}  // namespace tc
+}  // namespace emg
+
+// Launch hook for the slab solve (declared in emg_krylov.cuh).
+namespace emg {
+int tc_slab_product(int64_t w, int64_t row0, int64_t Bc, const void* groups, int G, int maxcol, const float2* Sinv,
+                    int64_t totD, int64_t offD, const float2* Y, float alpha, int beta, float2* Out, int32_t* status,
+                    cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        EMG_CUDA(cudaFuncSetAttribute(tc::k_cgemm_tf32, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::kCxSmem + 1024));
+        attr = true;
+    }
+    const dim3 grid((unsigned)((maxcol + tc::kN - 1) / tc::kN), (unsigned)((w + tc::kM - 1) / tc::kM), (unsigned)G);
+    tc::k_cgemm_tf32<<<grid, tc::kThreads, tc::kCxSmem + 1024, st>>>(
+        w, row0, Bc, static_cast<const tc::TcGroup*>(groups), Sinv, totD, offD, Y, alpha, beta, Out, status);
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+}  // namespace emg
+
+extern "C" int emg_tc_gemm_tf32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B,
+                                int64_t ldb, float* D, int64_t ldd, int32_t* status, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(A && B && D && status && M > 0 && N > 0 && K > 0 && lda >= K && ldb >= K && ldd >= N,
+                  "emg_tc_gemm_tf32: bad argument");
+    const dim3 grid((unsigned)((N + tc::kN - 1) / tc::kN), (unsigned)((M + tc::kM - 1) / tc::kM));
+    tc::k_gemm_tf32<<<grid, tc::kThreads, 0, (cudaStream_t)stream>>>(M, N, K, A, lda, B, ldb, D, ldd, status);
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}

@@ -213,6 +213,11 @@ class SlabFactor:
                 pass
             self._h = None
 
+    def set_tensor_cores(self, on: bool = True) -> None:
+        """Run the wide-group dense products of FP32-factor solves on the tcgen05 tensor
+        cores (TF32 products, FP32 accumulation)."""
+        _lib.call("emg_slab_set_tensor_cores", self._h, int(bool(on)))
+
     def info(self) -> dict:
         v = np.zeros(8, dtype=np.int64)
         _lib.call("emg_slab_info", self._h, v.ctypes.data_as(ctypes.c_void_p))
@@ -672,16 +677,19 @@ class FrequencySweep:
         """Initial guesses from the warm-start MLP trained on the converged columns Xs.
 
         Targets are the coefficients of each training column in the orthonormal basis
-        of span(Xs) (real and imaginary parts, normalised); the network maps
+        of span(Xs) (real and imaginary parts, each standardised); the network maps
         (normalised frequency, port) to them.  Returns (X0, final training loss)."""
         from .mlp import MLP, features
         Q, _ = torch.linalg.qr(Xs)
         Q = Q.contiguous()
         npo = len(self.ports)
         Y = (Q.conj().T @ Xs).T                                           # (nt*np, r) complex
-        T = torch.cat([Y.real, Y.imag], dim=1).to(torch.float32)
-        scale = T.abs().max().clamp_min(1e-30)
-        T = (T / scale).contiguous()
+        T = torch.cat([Y.real, Y.imag], dim=1)
+        # each output standardised on its own: the basis coefficients span orders of
+        # magnitude, and one common scale would leave the small ones unlearned
+        mu = T.mean(dim=0, keepdim=True)
+        scale = T.std(dim=0, keepdim=True).clamp_min(1e-30 + 1e-12 * T.abs().max().item())
+        T = ((T - mu) / scale).to(torch.float32).contiguous()
         f_lo, f_hi = float(np.min(freqs)), float(np.max(freqs))
         fn = lambda f: 2 * (np.asarray(f, dtype=float) - f_lo) / max(f_hi - f_lo, 1e-30) - 1   # noqa: E731
         tf = np.asarray(train_freqs, dtype=float)
@@ -690,7 +698,7 @@ class FrequencySweep:
         net = MLP(xt.shape[1], T.shape[1], max_batch=max(64, len(xt), len(fq) * npo), seed=seed, device=self.device)
         hist = net.fit(torch.as_tensor(xt), T, steps=steps, lr=3e-3)
         xa = features(np.repeat(fn(fq), npo), np.tile(np.arange(npo), len(fq)), npo)
-        P = net.forward(torch.as_tensor(xa)).to(torch.float64) * scale    # (nf*np, 2r)
+        P = net.forward(torch.as_tensor(xa)).to(torch.float64) * scale + mu    # (nf*np, 2r)
         r = Q.shape[1]
         yc = torch.complex(P[:, :r], P[:, r:])
         return (Q @ yc.T).contiguous(), hist[-1]

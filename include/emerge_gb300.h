@@ -217,6 +217,12 @@ int emg_slab_factor(emg_slab* slab, int precision, int64_t F, const int32_t* ama
 /* X_out = A_f^-1 X_in column by column, f = cfac[c] (HOST int32, Bc); X_in and
  * X_out are distinct DEVICE [n_solve][Bc] complex arrays. */
 int emg_slab_apply(emg_slab* slab, int64_t Bc, const int32_t* cfac, const double* X_in, double* X_out, void* stream);
+/* on != 0: the dense products of FP32-factor solves over column groups of at least
+ * 48 columns run on the tcgen05 tensor cores (TF32 products, FP32 accumulation);
+ * the slab solve is a preconditioner, so the TF32 rounding only adds to the FP32
+ * factor's own error.  Default off. */
+int emg_slab_set_tensor_cores(emg_slab* slab, int on);
+
 /* Flexible GMRES (FGMRES, restart <= 256) right-preconditioned by the slab
  * factors: column c solves A[:, cmat[c]] x = rhs with factor cfac[c] (HOST).  The
  * residual is FP64 throughout; with FP32 factors this is the mixed-precision
@@ -242,6 +248,14 @@ int emg_gmres_slab_mixed(const emg_rplan* plan, emg_slab* slab, int64_t Bc, cons
 int emg_gmres_slab_family(const emg_rplan* plan, emg_slab* slab, int64_t Bc, int nfam, const double* fam,
                           const double* coef, const int32_t* cfac, const double* rhs, double* x, int restart,
                           int max_iter, double tol, int32_t* iters_out, double* resid_out, void* stream);
+
+/* D = A B^T on the 5th-generation tensor cores (tcgen05.mma kind::tf32, FP32
+ * accumulation in tensor memory): A (M x K, ld lda), B (N x K, ld ldb), D (M x N,
+ * ld ldd), row-major FP32 DEVICE arrays; TF32 products (10-bit mantissa).
+ * *status (DEVICE int32, set to 0 by the caller) becomes 1 if a tile's bounded
+ * wait on its tensor-core work ran out. */
+int emg_tc_gemm_tf32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
+                     float* D, int64_t ldd, int32_t* status, void* stream);
 
 /* ------------------------------------------------------ warm-start MLP ---
  * No counterpart in the reference (a sweep acceleration).  A multilayer

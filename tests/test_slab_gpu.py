@@ -170,3 +170,27 @@ def test_mixed_precision_refinement_reaches_fp64_accuracy(system):
     for c in range(4):
         ref = spla.spsolve(Ks[c // 2].tocsc(), B[:, c])
         assert np.linalg.norm(x[:, c] - ref) / np.linalg.norm(ref) <= 1e-7
+
+
+def test_tensor_core_slab_products(system):
+    """Wide-group products of an FP32-factor solve on the tcgen05 tensor cores (TF32):
+    within TF32 rounding of the CUDA-core result, and FGMRES still reaches 1e-10."""
+    torch, sysr, slab, Ks, rhs, vals = system
+    slab.factor(vals, [0, 1], "fp32")
+    rng = np.random.default_rng(11)
+    n = Ks[0].shape[0]
+    B = rng.standard_normal((n, 70)) + 1j * rng.standard_normal((n, 70))
+    Bt = torch.as_tensor(B, device="cuda")
+    cf = [0] * 60 + [1] * 10
+    slab.set_tensor_cores(False)
+    ref = slab.apply(Bt, cf).cpu().numpy()
+    slab.set_tensor_cores(True)
+    try:
+        got = slab.apply(Bt, cf).cpu().numpy()
+        err = np.linalg.norm(got - ref, axis=0) / np.linalg.norm(ref, axis=0)
+        assert np.max(err) < 3e-2 and np.median(err) < 1e-2
+        cmat = torch.zeros(60, dtype=torch.int32, device="cuda")
+        x, its, res = slab.gmres(vals, Bt[:, :60].contiguous(), cmat, [0] * 60, tol=1e-10, restart=40, max_iter=400)
+        assert np.all(res <= 1e-10)
+    finally:
+        slab.set_tensor_cores(False)
