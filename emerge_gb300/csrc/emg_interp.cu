@@ -1,0 +1,147 @@
+// Second-order Nedelec field evaluation at arbitrary points: the GPU counterpart of
+// ned2_tet_interp (fem/mth/tet.py:372-497), which EMerge uses for the S-parameter
+// surface integrals (all_port_tets, fem/physics/edm/emfreq3d.py:648-653,703) and for
+// field output.
+//
+// Thread per point.  Location follows the reference: a point belongs to a tet of
+// ``tetids`` when its local coordinates xi = [v2-v1, v3-v1, v4-v1]^-1 (p - v1)
+// satisfy xi >= -1e-6 and sum(xi) <= 1 + 1e-8, and the last such tet in list
+// order wins (the reference overwrites in tet order), so the scan runs backwards
+// and stops at the first hit.  Field: with the barycentric numerators
+// A_i = a_i + b_i x + c_i y + d_i z = det(P) lambda_i (P rows (1, x_j, y_j, z_j))
+// and 216 V^3 = |det P|^3,
+//   edge (vertices 1, 2, length L):  L (e1 A1 + e2 A2)(g1 A2 - g2 A1) / 216 V^3
+//   face (vertices 1, 2, 3):         (-e1 |v1v3| (g1 A3 - g3 A1) A2
+//                                     + e2 |v1v2| (g1 A2 - g2 A1) A3) / 216 V^3
+// for g = b, c, d (x, y, z components), vertices in the mesh's edges/tris order.
+#include "emg_common.cuh"
+
+namespace emg {
+namespace interp {
+
+__device__ __forceinline__ double det3(double a, double b, double c, double d, double e, double f, double g, double h,
+                                       double i) {
+    return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+}
+
+__device__ __forceinline__ int local_of(const int32_t* tv, int32_t gid) {
+    return tv[0] == gid ? 0 : tv[1] == gid ? 1 : tv[2] == gid ? 2 : 3;
+}
+
+__global__ void k_interp(int64_t np_, const double* __restrict__ pts, const double* __restrict__ nodes, int64_t nN,
+                         const int32_t* __restrict__ tets, int64_t nT, const int32_t* __restrict__ edges, int64_t nE,
+                         const int32_t* __restrict__ tris, int64_t nTri, const int32_t* __restrict__ t2f,
+                         const double2* __restrict__ sol, int64_t ntl, const int32_t* __restrict__ tetids,
+                         double2* __restrict__ E) {
+    const int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (ip >= np_) return;
+    const double px = pts[ip], py = pts[np_ + ip], pz = pts[2 * np_ + ip];
+    double2 ex = make_double2(0, 0), ey = ex, ez = ex;
+    for (int64_t it = ntl - 1; it >= 0; --it) {
+        const int64_t t = tetids[it];
+        if (t < 0 || t >= nT) continue;
+        int32_t tv[4];
+        double vx[4], vy[4], vz[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            tv[j] = tets[j * nT + t];
+            vx[j] = nodes[tv[j]];
+            vy[j] = nodes[nN + tv[j]];
+            vz[j] = nodes[2 * nN + tv[j]];
+        }
+        // local coordinates: solve [e1 e2 e3] xi = p - v1 by Cramer's rule
+        const double e1x = vx[1] - vx[0], e1y = vy[1] - vy[0], e1z = vz[1] - vz[0];
+        const double e2x = vx[2] - vx[0], e2y = vy[2] - vy[0], e2z = vz[2] - vz[0];
+        const double e3x = vx[3] - vx[0], e3y = vy[3] - vy[0], e3z = vz[3] - vz[0];
+        const double qx = px - vx[0], qy = py - vy[0], qz = pz - vz[0];
+        const double dm = det3(e1x, e2x, e3x, e1y, e2y, e3y, e1z, e2z, e3z);
+        if (dm == 0.0) continue;
+        const double x0 = det3(qx, e2x, e3x, qy, e2y, e3y, qz, e2z, e3z) / dm;
+        const double x1 = det3(e1x, qx, e3x, e1y, qy, e3y, e1z, qz, e3z) / dm;
+        const double x2 = det3(e1x, e2x, qx, e1y, e2y, qy, e1z, e2z, qz) / dm;
+        if (!(x0 + x1 + x2 <= 1.00000001 && x0 >= -1e-6 && x1 >= -1e-6 && x2 >= -1e-6)) continue;
+        // barycentric numerators A_i(p) = det(P_i(p)), P_i = P with row i -> (1, p).
+        // Moving row i to the top and subtracting it: det(P_i(p)) = (-1)^i det[v_j - p;
+        // v_k - p; v_l - p] with (j, k, l) the other vertices in cyclic order (an even
+        // permutation of ascending order), and grad det[a - p; b - p; c - p] =
+        // -(b - a) x (c - a), so the coefficients (b_i, c_i, d_i) = -(-1)^i (v_k - v_j)
+        // x (v_l - v_j).  det(P) = det[e1; e2; e3] = dm.
+        double A[4], gb[4], gc[4], gd[4];
+        const double detP = dm;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int j = (i + 1) & 3, k = (i + 2) & 3, l = (i + 3) & 3;
+            const double s = (i & 1) ? -1.0 : 1.0;
+            const double ax = vx[j] - px, ay = vy[j] - py, az = vz[j] - pz;
+            const double bx = vx[k] - px, by = vy[k] - py, bz = vz[k] - pz;
+            const double cx = vx[l] - px, cy = vy[l] - py, cz = vz[l] - pz;
+            A[i] = s * det3(ax, bx, cx, ay, by, cy, az, bz, cz);
+            gb[i] = -s * ((vy[k] - vy[j]) * (vz[l] - vz[j]) - (vz[k] - vz[j]) * (vy[l] - vy[j]));
+            gc[i] = -s * ((vz[k] - vz[j]) * (vx[l] - vx[j]) - (vx[k] - vx[j]) * (vz[l] - vz[j]));
+            gd[i] = -s * ((vx[k] - vx[j]) * (vy[l] - vy[j]) - (vy[k] - vy[j]) * (vx[l] - vx[j]));
+        }
+        const double den = fabs(detP) * fabs(detP) * fabs(detP);
+        const int32_t* f = t2f + t;   // column t of (20, nT)
+        double2 rx = make_double2(0, 0), ry = rx, rz = rx;
+        for (int ie = 0; ie < 6; ++ie) {
+            const int32_t eid = f[ie * nT];
+            const int i1 = local_of(tv, edges[eid]), i2 = local_of(tv, edges[nE + eid]);
+            const double L = sqrt((vx[i1] - vx[i2]) * (vx[i1] - vx[i2]) + (vy[i1] - vy[i2]) * (vy[i1] - vy[i2]) +
+                                  (vz[i1] - vz[i2]) * (vz[i1] - vz[i2]));
+            const double2 e1 = sol[f[ie * nT]], e2 = sol[f[(10 + ie) * nT]];
+            const double2 sv = make_double2(e1.x * A[i1] + e2.x * A[i2], e1.y * A[i1] + e2.y * A[i2]);
+            const double wx = L * (gb[i1] * A[i2] - gb[i2] * A[i1]) / den;
+            const double wy = L * (gc[i1] * A[i2] - gc[i2] * A[i1]) / den;
+            const double wz = L * (gd[i1] * A[i2] - gd[i2] * A[i1]) / den;
+            rx.x += sv.x * wx; rx.y += sv.y * wx;
+            ry.x += sv.x * wy; ry.y += sv.y * wy;
+            rz.x += sv.x * wz; rz.y += sv.y * wz;
+        }
+        for (int jf = 0; jf < 4; ++jf) {
+            const int64_t fid = f[(6 + jf) * nT] - nE;
+            const int i1 = local_of(tv, tris[fid]), i2 = local_of(tv, tris[nTri + fid]),
+                      i3 = local_of(tv, tris[2 * nTri + fid]);
+            const double L1 = sqrt((vx[i1] - vx[i3]) * (vx[i1] - vx[i3]) + (vy[i1] - vy[i3]) * (vy[i1] - vy[i3]) +
+                                   (vz[i1] - vz[i3]) * (vz[i1] - vz[i3]));
+            const double L2 = sqrt((vx[i1] - vx[i2]) * (vx[i1] - vx[i2]) + (vy[i1] - vy[i2]) * (vy[i1] - vy[i2]) +
+                                   (vz[i1] - vz[i2]) * (vz[i1] - vz[i2]));
+            const double2 e1 = sol[f[(6 + jf) * nT]], e2 = sol[f[(16 + jf) * nT]];
+            const double* g[3] = {gb, gc, gd};
+            double w1[3], w2[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                w1[d] = -L1 * (g[d][i1] * A[i3] - g[d][i3] * A[i1]) * A[i2] / den;
+                w2[d] = L2 * (g[d][i1] * A[i2] - g[d][i2] * A[i1]) * A[i3] / den;
+            }
+            rx.x += e1.x * w1[0] + e2.x * w2[0]; rx.y += e1.y * w1[0] + e2.y * w2[0];
+            ry.x += e1.x * w1[1] + e2.x * w2[1]; ry.y += e1.y * w1[1] + e2.y * w2[1];
+            rz.x += e1.x * w1[2] + e2.x * w2[2]; rz.y += e1.y * w1[2] + e2.y * w2[2];
+        }
+        ex = rx;
+        ey = ry;
+        ez = rz;
+        break;
+    }
+    E[ip] = ex;
+    E[np_ + ip] = ey;
+    E[2 * np_ + ip] = ez;
+}
+
+}  // namespace interp
+}  // namespace emg
+
+extern "C" int emg_field_interp(int64_t n_points, const double* points, int64_t n_nodes, const double* nodes,
+                                int64_t n_tets, const int32_t* tets, int64_t n_edges, const int32_t* edges,
+                                int64_t n_tris, const int32_t* tris, const int32_t* tet_to_field, const double* solution,
+                                int64_t n_tetids, const int32_t* tetids, double* E_out, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(points && nodes && tets && edges && tris && tet_to_field && solution && E_out && n_points >= 0 &&
+                      n_tetids >= 0 && (n_tetids == 0 || tetids),
+                  "emg_field_interp: bad argument");
+    if (n_points == 0) return EMG_OK;
+    interp::k_interp<<<(unsigned)((n_points + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+        n_points, points, nodes, n_nodes, tets, n_tets, edges, n_edges, tris, n_tris, tet_to_field,
+        reinterpret_cast<const double2*>(solution), n_tetids, tetids, reinterpret_cast<double2*>(E_out));
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}

@@ -548,7 +548,6 @@ __global__ void k_narrow(int64_t nv, const double2* __restrict__ in, float2* __r
 // Out[r, cols of group g] = beta Out + alpha S_i^-1[r, :] Y[:, cols]: warp per row,
 // lanes over the row of S_i^-1 (coalesced), 16 columns per pass.  Grid: row blocks x groups.
 constexpr int kRowCols = 16;
-constexpr int kWideGroup = 48;     // groups at least this wide use the tiled product
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_rowmv(int64_t w, int64_t row0, int64_t Bc, const Group* __restrict__ groups,
                                                     const typename C2<R>::T* __restrict__ Sinv, int64_t totD, int64_t offD,
@@ -713,6 +712,7 @@ struct emg_slab {
     int32_t* kcnt = nullptr;          // per-tile arrival counters (zero between launches)
     int64_t kcnt_n = 0;
     int use_tc = 0;                   // wide-group products of FP32 factors on the tcgen05 tensor cores
+    int wide = 48;                    // column groups at least this wide use the tiled products
     int32_t* tc_status = nullptr;     // set by a tensor-core tile whose bounded wait ran out
 };
 
@@ -1100,7 +1100,7 @@ struct SlabPrecond : emg::Precond {
         // split-K scratch for the wide-group products (largest need over the slabs)
         int maxcol = 0;
         for (const auto& g : groups) maxcol = std::max(maxcol, (int)g.ncol);
-        if (maxcol >= emg::slab::kWideGroup) {
+        if (maxcol >= s->wide) {
             const int64_t ct = (maxcol + emg::slab::kTile - 1) / emg::slab::kTile, G = (int64_t)groups.size();
             size_t need = 0;
             int64_t tiles_max = 0;
@@ -1159,7 +1159,7 @@ struct SlabPrecond : emg::Precond {
         // dense slab product: warp-per-row for narrow groups, 64 x 64 tiles for wide ones
         auto dense = [&](int64_t w, int64_t i, R alpha, int beta) {
             if constexpr (sizeof(R) == 4) {
-                if (s->use_tc && maxcol >= kWideGroup) {
+                if (s->use_tc && maxcol >= s->wide) {
                     emg::tc_slab_product(w, s->off[i], Bc, s->groups, (int)G, maxcol,
                                          reinterpret_cast<const float2*>(Sinv), s->totD, s->offD[i],
                                          reinterpret_cast<const float2*>(Y), (float)alpha, beta,
@@ -1167,7 +1167,7 @@ struct SlabPrecond : emg::Precond {
                     return;
                 }
             }
-            if (maxcol >= kWideGroup) {
+            if (maxcol >= s->wide) {
                 const int64_t ct = (maxcol + kTile - 1) / kTile, rt = (w + kTile - 1) / kTile;
                 const int sp = gemm_splits(ct * rt * G, w);
                 k_slab_gemm<R><<<dim3((unsigned)ct, (unsigned)(rt * sp), G), kThreads, 0, st>>>(
@@ -1248,6 +1248,12 @@ extern "C" int emg_gmres_slab(const emg_rplan* pc, emg_slab* s, int64_t Bc, cons
 extern "C" int emg_slab_set_tensor_cores(emg_slab* s, int on) {
     EMG_CHECK_ARG(s, "emg_slab_set_tensor_cores: NULL argument");
     s->use_tc = on ? 1 : 0;
+    return EMG_OK;
+}
+
+extern "C" int emg_slab_set_wide_group(emg_slab* s, int min_columns) {
+    EMG_CHECK_ARG(s && min_columns >= 1, "emg_slab_set_wide_group: bad argument");
+    s->wide = min_columns;
     return EMG_OK;
 }
 

@@ -218,6 +218,10 @@ class SlabFactor:
         cores (TF32 products, FP32 accumulation)."""
         _lib.call("emg_slab_set_tensor_cores", self._h, int(bool(on)))
 
+    def set_wide_group(self, min_columns: int) -> None:
+        """Column groups of at least ``min_columns`` use the tiled dense products."""
+        _lib.call("emg_slab_set_wide_group", self._h, int(min_columns))
+
     def info(self) -> dict:
         v = np.zeros(8, dtype=np.int64)
         _lib.call("emg_slab_info", self._h, v.ctypes.data_as(ctypes.c_void_p))

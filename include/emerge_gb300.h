@@ -178,6 +178,19 @@ int emg_gmres(const emg_rplan* plan, int64_t Bc, const int32_t* cmat, int64_t Bm
               const double* rhs, double* x, int restart, int max_iter, double tol, int32_t* iters_out,
               double* resid_out, void* stream);
 
+/* ---------------------------------------------------- field evaluation ---
+ * Second-order Nedelec field at arbitrary points, the counterpart of
+ * ned2_tet_interp (fem/mth/tet.py:372-497).  points (3, n_points) row-major
+ * (x[], y[], z[]); nodes (3, n_nodes); tets (4, n_tets), edges (2, n_edges), tris
+ * (3, n_tris), tet_to_field (20, n_tets) int32; solution complex (n_field);
+ * tetids (n_tetids) the tets searched, the last containing tet in list order
+ * winning as in the reference; E_out (3, n_points) complex (zero where no tet
+ * contains the point).  All DEVICE arrays. */
+int emg_field_interp(int64_t n_points, const double* points, int64_t n_nodes, const double* nodes, int64_t n_tets,
+                     const int32_t* tets, int64_t n_edges, const int32_t* edges, int64_t n_tris, const int32_t* tris,
+                     const int32_t* tet_to_field, const double* solution, int64_t n_tetids, const int32_t* tetids,
+                     double* E_out, void* stream);
+
 /* ------------------------------------------------------- slab solver ---
  * Direct block-tridiagonal factorization of the restricted system, the
  * counterpart of the reference's direct solvers (SolverSuperLU / SolverPardiso /
@@ -217,11 +230,14 @@ int emg_slab_factor(emg_slab* slab, int precision, int64_t F, const int32_t* ama
 /* X_out = A_f^-1 X_in column by column, f = cfac[c] (HOST int32, Bc); X_in and
  * X_out are distinct DEVICE [n_solve][Bc] complex arrays. */
 int emg_slab_apply(emg_slab* slab, int64_t Bc, const int32_t* cfac, const double* X_in, double* X_out, void* stream);
-/* on != 0: the dense products of FP32-factor solves over column groups of at least
- * 48 columns run on the tcgen05 tensor cores (TF32 products, FP32 accumulation);
+/* on != 0: the dense products of FP32-factor solves over wide column groups (see
+ * emg_slab_set_wide_group) run on the tcgen05 tensor cores (TF32 products, FP32 accumulation);
  * the slab solve is a preconditioner, so the TF32 rounding only adds to the FP32
  * factor's own error.  Default off. */
 int emg_slab_set_tensor_cores(emg_slab* slab, int on);
+/* Column groups of at least min_columns use 64 x 64 tiled dense products (with
+ * split-K), narrower ones a warp per row.  Default 48. */
+int emg_slab_set_wide_group(emg_slab* slab, int min_columns);
 
 /* Flexible GMRES (FGMRES, restart <= 256) right-preconditioned by the slab
  * factors: column c solves A[:, cmat[c]] x = rhs with factor cfac[c] (HOST).  The

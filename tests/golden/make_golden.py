@@ -21,6 +21,10 @@ Fixtures:
                      fem/physics/edm/emfreq3d.py:607-779)
   waveguide_abc.npz  the same guide with port 2 replaced by an AbsorbingBoundary:
                      K row checksums, solve_ids, port vector at 10 GHz
+  interp.npz         ned2_tet_interp (fem/mth/tet.py:372-497) of the guide's 10 GHz
+                     SuperLU field: 6-point quadrature points of the port-1 triangles
+                     over the port tets (the S-parameter evaluation) and random
+                     interior points over all tets
 """
 from __future__ import annotations
 
@@ -302,8 +306,39 @@ def make_waveguide_abc():
     print("waveguide_abc: ok")
 
 
+def make_interp():
+    """Reference field interpolation of the waveguide fixture's 10 GHz port-1 solution."""
+    z = np.load(os.path.join(HERE, "waveguide.npz"))
+    tm, (a, b, L) = waveguide_mesh()
+    m = reference_mesh(tm)
+    field = Nedelec2(m)
+    sol = z["x1_1"]
+    rng = np.random.default_rng(21)
+    # port-1 quadrature points (6-point Dunavant rule, as the S-parameter integral uses)
+    D = ref_opt.gaus_quad_tri(4)
+    tri = np.asarray(z["port_tris_1"], dtype=np.int64)
+    tv = m.tris[:, tri]
+    v1, v2, v3 = m.nodes[:, tv[0]], m.nodes[:, tv[1]], m.nodes[:, tv[2]]
+    pts = []
+    for k in range(D.shape[1]):
+        pts.append(v1 * D[1, k] + v2 * D[2, k] + v3 * D[3, k])
+    port_pts = np.concatenate(pts, axis=1)
+    # interior points: a random barycentric point of 300 random tets
+    tsel = rng.choice(m.n_tets, 300, replace=False)
+    lam = rng.dirichlet(np.ones(4), size=300).T * 0.9 + 0.025
+    lam /= lam.sum(axis=0)
+    inner = np.einsum("vt,dvt->dt", lam, m.nodes[:, m.tets[:, tsel]])
+    port_tets = np.asarray(z["port_tets"], dtype=np.int64)
+    t0 = time.time()
+    Ep = field.interpolate(sol, port_pts[0], port_pts[1], port_pts[2], tetids=port_tets)
+    Ei = field.interpolate(sol, inner[0], inner[1], inner[2], tetids=np.arange(m.n_tets, dtype=np.int64))
+    print(f"interp: {port_pts.shape[1]} port points, {inner.shape[1]} interior points ({time.time() - t0:.1f} s)")
+    np.savez_compressed(os.path.join(HERE, "interp.npz"), port_points=port_pts, port_tets=port_tets,
+                        port_E=np.stack(Ep), inner_points=inner, inner_E=np.stack(Ei), inner_tets=tsel)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc"]
+    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc", "interp"]
     if "tet" in which:
         make_tet_elements()
     if "tri" in which:
@@ -314,3 +349,5 @@ if __name__ == "__main__":
         make_waveguide()
     if "abc" in which:
         make_waveguide_abc()
+    if "interp" in which:
+        make_interp()
