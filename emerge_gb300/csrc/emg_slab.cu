@@ -712,7 +712,7 @@ struct emg_slab {
     int32_t* kcnt = nullptr;          // per-tile arrival counters (zero between launches)
     int64_t kcnt_n = 0;
     int use_tc = 0;                   // wide-group products of FP32 factors on the tcgen05 tensor cores
-    int wide = 48;                    // column groups at least this wide use the tiled products
+    int wide = 8;                     // column groups at least this wide use the tiled products
     int32_t* tc_status = nullptr;     // set by a tensor-core tile whose bounded wait ran out
 };
 

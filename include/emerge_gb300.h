@@ -236,7 +236,8 @@ int emg_slab_apply(emg_slab* slab, int64_t Bc, const int32_t* cfac, const double
  * factor's own error.  Default off. */
 int emg_slab_set_tensor_cores(emg_slab* slab, int on);
 /* Column groups of at least min_columns use 64 x 64 tiled dense products (with
- * split-K), narrower ones a warp per row.  Default 48. */
+ * split-K), narrower ones a warp per row.  Default 8: the tiled products are faster
+ * even for 8-column groups (measured 80 vs 156 ms per solve on the 2 mm iris). */
 int emg_slab_set_wide_group(emg_slab* slab, int min_columns);
 
 /* Flexible GMRES (FGMRES, restart <= 256) right-preconditioned by the slab
