@@ -317,6 +317,9 @@ def run_sweep(args):
     out = {"workload": f"{p.name}: N={p.field.n_field} DOFs ({sw.sys.n} after PEC), {nf} points 8-12 GHz x 2 ports",
            "metric": "sweep freq-pts/s", "tol": args.sweep_tol, "setup_s": round(setup, 2),
            "slabs": sl.info()["slabs"], "max_slab_width": sl.info()["max_width"], "chunk_points": chunk}
+    # the slab products' layout, tuned once per mesh and column pattern (not timed)
+    out["autotune"] = sw.autotune(freqs, n_anchor=args.sweep_anchors, chunk=chunk)
+    out["autotune"]["seconds"] = round(out["autotune"]["seconds"], 2)
     with ClockSampler(0) as clk:
         # warm-up of every code path on a tiny sweep (graph capture, cuBLAS/cuSOLVER handles)
         sw.run_warm(freqs[:4], n_train=2, solver="anchored", n_anchor=1, precision="fp32", guess="mlp",

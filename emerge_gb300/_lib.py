@@ -57,6 +57,7 @@ SIGNATURES = {
     "emg_tc_gemm_tf32": (ctypes.c_int, [c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp]),
     "emg_slab_set_tensor_cores": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "emg_slab_set_wide_group": (ctypes.c_int, [c_vp, ctypes.c_int]),
+    "emg_slab_set_max_splits": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "emg_field_interp": (ctypes.c_int, [c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp,
                                         c_i64, c_vp, c_vp, c_vp]),
     "emg_slab_create": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, ctypes.POINTER(c_vp)]),

@@ -669,11 +669,11 @@ __global__ void __launch_bounds__(kThreads) k_slab_gemm(int64_t w, int64_t row0,
 }
 
 // K splits of a wide-group product: enough CTAs for two per SM, at least 256
-// columns of K per split, at most 8.
-inline int gemm_splits(int64_t tiles, int64_t w) {
+// columns of K per split, at most max_splits (8 unless tuned).
+inline int gemm_splits(int64_t tiles, int64_t w, int max_splits = 8) {
     int64_t sp = (2 * 152 + tiles - 1) / std::max<int64_t>(tiles, 1);
     sp = std::min<int64_t>(sp, std::max<int64_t>(1, w / 256));
-    return (int)std::max<int64_t>(1, std::min<int64_t>(sp, 8));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(sp, std::max(1, max_splits)));
 }
 
 }  // namespace slab
@@ -713,6 +713,7 @@ struct emg_slab {
     int64_t kcnt_n = 0;
     int use_tc = 0;                   // wide-group products of FP32 factors on the tcgen05 tensor cores
     int wide = 8;                     // column groups at least this wide use the tiled products
+    int max_splits = 8;               // split-K cap of the tiled products
     int32_t* tc_status = nullptr;     // set by a tensor-core tile whose bounded wait ran out
 };
 
@@ -1107,7 +1108,7 @@ struct SlabPrecond : emg::Precond {
             for (int i = 0; i < s->m; ++i) {
                 const int64_t w = s->off[i + 1] - s->off[i];
                 const int64_t tiles = ct * ((w + emg::slab::kTile - 1) / emg::slab::kTile) * G;
-                const int sp = emg::slab::gemm_splits(tiles, w);
+                const int sp = emg::slab::gemm_splits(tiles, w, s->max_splits);
                 tiles_max = std::max(tiles_max, tiles);
                 if (sp > 1)
                     need = std::max(need, (size_t)tiles * sp * emg::slab::kTile * emg::slab::kTile *
@@ -1169,7 +1170,7 @@ struct SlabPrecond : emg::Precond {
             }
             if (maxcol >= s->wide) {
                 const int64_t ct = (maxcol + kTile - 1) / kTile, rt = (w + kTile - 1) / kTile;
-                const int sp = gemm_splits(ct * rt * G, w);
+                const int sp = gemm_splits(ct * rt * G, w, s->max_splits);
                 k_slab_gemm<R><<<dim3((unsigned)ct, (unsigned)(rt * sp), G), kThreads, 0, st>>>(
                     w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, alpha, beta, Z, sp,
                     static_cast<T*>(s->kpart), s->kcnt);
@@ -1254,6 +1255,12 @@ extern "C" int emg_slab_set_tensor_cores(emg_slab* s, int on) {
 extern "C" int emg_slab_set_wide_group(emg_slab* s, int min_columns) {
     EMG_CHECK_ARG(s && min_columns >= 1, "emg_slab_set_wide_group: bad argument");
     s->wide = min_columns;
+    return EMG_OK;
+}
+
+extern "C" int emg_slab_set_max_splits(emg_slab* s, int max_splits) {
+    EMG_CHECK_ARG(s && max_splits >= 1 && max_splits <= 16, "emg_slab_set_max_splits: bad argument");
+    s->max_splits = max_splits;
     return EMG_OK;
 }
 

@@ -221,6 +221,39 @@ class SlabFactor:
     def set_wide_group(self, min_columns: int) -> None:
         """Column groups of at least ``min_columns`` use the tiled dense products."""
         _lib.call("emg_slab_set_wide_group", self._h, int(min_columns))
+        self._wide = int(min_columns)
+
+    def set_max_splits(self, max_splits: int) -> None:
+        """Cap on the split-K factor of the tiled dense products."""
+        _lib.call("emg_slab_set_max_splits", self._h, int(max_splits))
+        self._splits = int(max_splits)
+
+    def autotune(self, columns: int, cfac, repeats: int = 3, candidates=None) -> dict:
+        """Pick the product layout for solves of ``columns`` columns with factor map
+        ``cfac`` by timing them: the wide-group threshold (tiled vs warp-per-row) and
+        the split-K cap.  Keeps the fastest setting; returns {setting: ms} and the
+        choice.  Run after ``factor``; the timed solves use random right-hand sides."""
+        cand = candidates or [(w, sp) for w in (1, 8, 48, 1 << 30) for sp in (1, 2, 4, 8)]
+        cf = np.ascontiguousarray(cfac, dtype=np.int32)
+        X = torch.randn((self.sys.n, int(columns)), dtype=torch.complex128, device=self.sys.device)
+        times = {}
+        for w, sp in cand:
+            self.set_wide_group(w)
+            self.set_max_splits(sp)
+            self.apply(X, cf)                                   # warm-up (allocations)
+            torch.cuda.synchronize()
+            best = float("inf")
+            for _ in range(repeats):
+                t0 = time.perf_counter()
+                self.apply(X, cf)
+                torch.cuda.synchronize()
+                best = min(best, time.perf_counter() - t0)
+            times[(w, sp)] = 1e3 * best
+        choice = min(times, key=times.get)
+        self.set_wide_group(choice[0])
+        self.set_max_splits(choice[1])
+        return {"times_ms": {f"wide={w},splits={sp}": round(t, 3) for (w, sp), t in times.items()},
+                "choice": {"wide": choice[0], "max_splits": choice[1]}}
 
     def info(self) -> dict:
         v = np.zeros(8, dtype=np.int64)
@@ -494,6 +527,22 @@ class FrequencySweep:
         torch.cuda.synchronize()
         self._slab_key = key
         return time.perf_counter() - t0
+
+    def autotune(self, freqs, n_anchor: int = 8, chunk: int | None = None, precision: str = "fp32") -> dict:
+        """Tune the slab products (``SlabFactor.autotune``) for this sweep's column
+        pattern: the anchors' factors and one chunk of (frequency, port) columns."""
+        freqs = np.asarray(freqs, dtype=float)
+        anchors = self.default_anchors(freqs, n_anchor)
+        self.factor_anchors(anchors, precision)
+        nf, npo = len(freqs), len(self.ports)
+        c = min(nf, chunk or nf)
+        near = np.argmin(np.abs(freqs[:c, None] - anchors[None, :]), axis=1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = self.slab().autotune(c * npo, np.repeat(near, npo),
+                                   candidates=[(w, sp) for w in (8, 1 << 30) for sp in (1, 4, 8)])
+        out["seconds"] = time.perf_counter() - t0
+        return out
 
     @staticmethod
     def default_anchors(freqs, n_anchor: int) -> np.ndarray:

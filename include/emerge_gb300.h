@@ -239,6 +239,9 @@ int emg_slab_set_tensor_cores(emg_slab* slab, int on);
  * split-K), narrower ones a warp per row.  Default 8: the tiled products are faster
  * even for 8-column groups (measured 80 vs 156 ms per solve on the 2 mm iris). */
 int emg_slab_set_wide_group(emg_slab* slab, int min_columns);
+/* Cap on the K splits of the tiled products (1..16; default 8).  The splits per
+ * slab are chosen for two CTAs per SM with at least 256 K columns each. */
+int emg_slab_set_max_splits(emg_slab* slab, int max_splits);
 
 /* Flexible GMRES (FGMRES, restart <= 256) right-preconditioned by the slab
  * factors: column c solves A[:, cmat[c]] x = rhs with factor cfac[c] (HOST).  The

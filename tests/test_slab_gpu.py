@@ -194,3 +194,18 @@ def test_tensor_core_slab_products(system):
         assert np.all(res <= 1e-10)
     finally:
         slab.set_tensor_cores(False)
+
+
+def test_autotune_picks_a_layout_and_solves_stay_exact(system):
+    torch, sysr, slab, Ks, rhs, vals = system
+    slab.factor(vals, [0, 1], "fp64")
+    cf = [0] * 24 + [1] * 8
+    out = slab.autotune(32, cf, repeats=1, candidates=[(8, 1), (8, 4), (1 << 30, 8)])
+    assert set(out["choice"]) == {"wide", "max_splits"} and len(out["times_ms"]) == 3
+    B = np.concatenate(rhs, axis=1)
+    X = slab.apply(torch.as_tensor(B, device="cuda"), [0, 0, 1, 1]).cpu().numpy()
+    for c in range(4):
+        ref = spla.spsolve(Ks[c // 2].tocsc(), B[:, c])
+        assert np.linalg.norm(X[:, c] - ref) / np.linalg.norm(ref) <= 1e-9
+    slab.set_wide_group(8)
+    slab.set_max_splits(8)
