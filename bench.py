@@ -329,8 +329,11 @@ def run_sweep(args):
                   refine=args.sweep_refine, inner=args.sweep_inner)
         fast = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored", n_anchor=args.sweep_anchors,
                            guess="mlp", mlp_steps=args.sweep_mlp_steps, **kw)
+        # every variant pays its own anchor factorization (the factors are cached per key)
+        sw._slab_key = None
         proj = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored", n_anchor=args.sweep_anchors,
                            guess="projection", **kw)
+        sw._slab_key = None
         cold = sw.run_anchored(freqs, n_anchor=args.sweep_anchors, **kw)
         plain = sw.run(freqs[idx], method="plain", precond="slab64", tol=args.sweep_tol)
     v_fast = nf / fast.seconds

@@ -28,6 +28,13 @@ SIGNATURES = {
     "emg_plan_pattern": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp]),
     "emg_assemble_tet": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "emg_assemble_tet_host": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "emg_assemble_tet_tensor": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "emg_topology_create": (ctypes.c_int, [c_i64, c_i64, c_vp, c_vp, c_vp]),
+    "emg_topology_sizes": (ctypes.c_int, [c_vp, c_vp, c_vp]),
+    "emg_topology_get": (ctypes.c_int, [c_vp] * 9),
+    "emg_topology_destroy": (None, [c_vp]),
+    "emg_edge_lengths": (ctypes.c_int, [c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "emg_assemble_tet_tensor_host": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "emg_plan_destroy": (None, [c_vp]),
     "emg_tri_robin_force": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            c_vp, c_vp, c_vp]),

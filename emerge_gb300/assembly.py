@@ -15,8 +15,10 @@ fem/physics/edm/assembler.py:319)::
     from emerge_gb300.assembly import tet_mass_stiffness_matrices
     oa.tet_mass_stiffness_matrices = tet_mass_stiffness_matrices
 
-Materials must be isotropic (εr and μr scalar multiples of the identity per
-tet); anything else raises ``NotImplementedError``.
+Materials: when εr and μr are scalar multiples of the identity in every tet the
+float-float fill runs (``emg_assemble_tet``); any other (3,3,nT) tensors go to
+the FP64 tensor fill (``emg_assemble_tet_tensor``) with Ms = matinv(μr) and
+Mm = εr per tet, as _matrix_builder passes them (optimized_assembly.py:95-108).
 """
 from __future__ import annotations
 
@@ -36,16 +38,59 @@ def _stream() -> ctypes.c_void_p:
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def scalar_material(m: np.ndarray, name: str) -> np.ndarray:
-    """Return the per-tet scalar of a (3,3,nT) material tensor that is s·I, else raise."""
+def _check_tensor(m: np.ndarray, name: str) -> np.ndarray:
     m = np.asarray(m)
     if m.ndim != 3 or m.shape[:2] != (3, 3):
         raise ValueError(f"{name} must have shape (3, 3, n_tets), got {m.shape}")
+    return m
+
+
+def is_scalar_material(m: np.ndarray) -> bool:
+    """True when every tet's (3,3) tensor is s·I."""
+    m = np.asarray(m)
     d = m[0, 0, :]
     off = np.abs(m[0, 1]) + np.abs(m[0, 2]) + np.abs(m[1, 0]) + np.abs(m[1, 2]) + np.abs(m[2, 0]) + np.abs(m[2, 1])
-    if np.any(off != 0) or np.any(m[1, 1] != d) or np.any(m[2, 2] != d):
-        raise NotImplementedError(f"the GPU assembler supports isotropic {name} (scalar times identity) only")
-    return d.astype(np.complex128)
+    return not (np.any(off != 0) or np.any(m[1, 1] != d) or np.any(m[2, 2] != d))
+
+
+def scalar_material(m: np.ndarray, name: str) -> np.ndarray:
+    """Return the per-tet scalar of a (3,3,nT) material tensor that is s·I, else raise."""
+    m = _check_tensor(m, name)
+    if not is_scalar_material(m):
+        raise ValueError(f"{name} is not a scalar multiple of the identity in every tet")
+    return m[0, 0, :].astype(np.complex128)
+
+
+def matinv_tensors(s: np.ndarray) -> np.ndarray:
+    """matinv (fem/mth/optimized.py:441-461) of every (3,3) slice of a (3,3,nT) array.
+
+    A tensor with all off-diagonal entries zero gets the reciprocal diagonal;
+    any other gets adj(s)·det(s), the reference's expression (it multiplies by
+    the determinant rather than dividing).
+    """
+    s = np.asarray(s, dtype=np.complex128)
+    out = np.zeros_like(s)
+    diag = ((s[0, 1] == 0) & (s[0, 2] == 0) & (s[1, 0] == 0) & (s[1, 2] == 0) & (s[2, 0] == 0) & (s[2, 1] == 0))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for k in range(3):
+            out[k, k] = np.where(diag, 1 / s[k, k], 0)
+    g = ~diag
+    if np.any(g):
+        a = s[:, :, g]
+        det = (a[0, 0] * a[1, 1] * a[2, 2] - a[0, 0] * a[1, 2] * a[2, 1] - a[0, 1] * a[1, 0] * a[2, 2]
+               + a[0, 1] * a[1, 2] * a[2, 0] + a[0, 2] * a[1, 0] * a[2, 1] - a[0, 2] * a[1, 1] * a[2, 0])
+        adj = np.empty_like(a)
+        adj[0, 0] = a[1, 1] * a[2, 2] - a[1, 2] * a[2, 1]
+        adj[0, 1] = -a[0, 1] * a[2, 2] + a[0, 2] * a[2, 1]
+        adj[0, 2] = a[0, 1] * a[1, 2] - a[0, 2] * a[1, 1]
+        adj[1, 0] = -a[1, 0] * a[2, 2] + a[1, 2] * a[2, 0]
+        adj[1, 1] = a[0, 0] * a[2, 2] - a[0, 2] * a[2, 0]
+        adj[1, 2] = -a[0, 0] * a[1, 2] + a[0, 2] * a[1, 0]
+        adj[2, 0] = a[1, 0] * a[2, 1] - a[1, 1] * a[2, 0]
+        adj[2, 1] = -a[0, 0] * a[2, 1] + a[0, 1] * a[2, 0]
+        adj[2, 2] = a[0, 0] * a[1, 1] - a[0, 1] * a[1, 0]
+        out[:, :, g] = adj * det
+    return out
 
 
 class AssemblyPlan:
@@ -128,6 +173,45 @@ class AssemblyPlan:
             _lib.call("emg_assemble_tet", self._plan, _dptr(eps), _dptr(mu_inv), _dptr(E), _dptr(B), _stream())
         return E, B
 
+    def assemble_tensor(self, eps9: torch.Tensor, mu_inv9: torch.Tensor, E: torch.Tensor | None = None,
+                        B: torch.Tensor | None = None):
+        """Device call for tensor materials: eps9, mu_inv9 complex128 (9, n_tets) CUDA tensors."""
+        if E is None:
+            E = torch.empty(max(self.nnz, 1), dtype=torch.complex128, device=self.device)
+        if B is None:
+            B = torch.empty(max(self.nnz, 1), dtype=torch.complex128, device=self.device)
+        for t in (eps9, mu_inv9):
+            assert t.dtype == torch.complex128 and t.is_contiguous() and tuple(t.shape) == (9, self.n_tets)
+        with torch.cuda.device(self.device):
+            _lib.call("emg_assemble_tet_tensor", self._plan, _dptr(eps9), _dptr(mu_inv9), _dptr(E), _dptr(B),
+                      _stream())
+        return E, B
+
+    def assemble_tensor_host(self, eps9: np.ndarray, mu_inv9: np.ndarray):
+        """Host call through emg_assemble_tet_tensor_host: (9, n_tets) complex numpy in, values out."""
+        eps9 = np.ascontiguousarray(eps9, dtype=np.complex128).reshape(9, self.n_tets)
+        mu_inv9 = np.ascontiguousarray(mu_inv9, dtype=np.complex128).reshape(9, self.n_tets)
+        E = np.empty(self.nnz, dtype=np.complex128)
+        B = np.empty(self.nnz, dtype=np.complex128)
+        with torch.cuda.device(self.device):
+            _lib.call("emg_assemble_tet_tensor_host", self._plan, eps9.ctypes.data_as(ctypes.c_void_p),
+                      mu_inv9.ctypes.data_as(ctypes.c_void_p), E.ctypes.data_as(ctypes.c_void_p),
+                      B.ctypes.data_as(ctypes.c_void_p), _stream())
+        return E, B
+
+    def assemble_materials(self, er: np.ndarray, ur: np.ndarray):
+        """Device values (E, B) for (3,3,nT) host material arrays; scalar or tensor fill as they require."""
+        er = _check_tensor(er, "er")
+        ur = _check_tensor(ur, "ur")
+        if is_scalar_material(er) and is_scalar_material(ur):
+            eps, mu_inv = material_scalars(er, ur)
+            return self.assemble(torch.as_tensor(eps, device=self.device),
+                                 torch.as_tensor(mu_inv, device=self.device))
+        eps9 = np.ascontiguousarray(er, dtype=np.complex128).reshape(9, -1)
+        mu9 = np.ascontiguousarray(matinv_tensors(ur)).reshape(9, -1)
+        return self.assemble_tensor(torch.as_tensor(eps9, device=self.device),
+                                    torch.as_tensor(mu9, device=self.device))
+
     def assemble_host(self, eps: np.ndarray, mu_inv: np.ndarray, E: np.ndarray | None = None,
                       B: np.ndarray | None = None):
         """Host call through emg_assemble_tet_host: numpy in, numpy out (copies inside the call)."""
@@ -167,8 +251,14 @@ def tet_mass_stiffness_matrices(field, er: np.ndarray, ur: np.ndarray):
     """Drop-in for fem/physics/edm/optimized_assembly.py:43-64 -> (E, B) scipy CSR, complex128."""
     from scipy.sparse import csr_matrix
     plan = plan_for(field)
-    eps, mu_inv = material_scalars(er, ur)
-    Ed, Bd = plan.assemble_host(eps, mu_inv)
+    er = _check_tensor(er, "er")
+    ur = _check_tensor(ur, "ur")
+    if is_scalar_material(er) and is_scalar_material(ur):
+        eps, mu_inv = material_scalars(er, ur)
+        Ed, Bd = plan.assemble_host(eps, mu_inv)
+    else:
+        Ed, Bd = plan.assemble_tensor_host(np.ascontiguousarray(er, dtype=np.complex128).reshape(9, -1),
+                                           matinv_tensors(ur).reshape(9, -1))
     ip, ix = plan.pattern_host()
     N = plan.n_field
     E = csr_matrix((Ed, ix, ip), shape=(N, N))

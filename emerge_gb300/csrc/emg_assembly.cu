@@ -70,6 +70,18 @@ struct __align__(16) TetRec {
     uint64_t lmap;     // local maps: edge slot e -> bits 4e (first vertex), 4e+2 (second);
                        // face slot f -> bits 24+6f, +2, +4 (tri vertices 0,1,2)
     int32_t dof[20];   // tet_to_field column
+    double G[12];      // cofactor vectors G_p = (b_p, c_p, d_p), p-major (tensor materials)
+};
+
+// Material-weighted invariants of one tet for tensor materials, one real part
+// (re or im) of the complex values: gram[p*4+q] = G_p . (Mm G_q) and
+// cdot[P*6+R] = X_P . (Ms X_R), X_P = G_a x G_b for vertex pair P = (a < b).
+constexpr int kTInv = 52;
+struct TView {
+    const double* len;
+    const double* ds;
+    uint64_t lmap;
+    const double* inv;
 };
 
 constexpr int kFillWarps = 4;
@@ -89,6 +101,15 @@ __device__ __forceinline__ double ccv(const TetRec& r, int p, int q, int s1, int
 }
 __device__ __forceinline__ double gv(const TetRec& r, int p, int q) { return r.gram[gi(p, q)]; }
 __device__ __forceinline__ double dsv(const TetRec& r, int p, int q) { return r.ds[c_pidx[p][q]]; }
+// The same accessors over ordered (row vertex, column vertex) tensor invariants.
+__device__ __forceinline__ double ccv(const TView& r, int p, int q, int s1, int s2) {
+    if (p == q || s1 == s2) return 0.0;
+    const int P = c_pidx[p][q], R = c_pidx[s1][s2];
+    const double sg = ((p < q) == (s1 < s2)) ? 1.0 : -1.0;
+    return sg * r.inv[16 + P * 6 + R];
+}
+__device__ __forceinline__ double gv(const TView& r, int p, int q) { return r.inv[p * 4 + q]; }
+__device__ __forceinline__ double dsv(const TView& r, int p, int q) { return r.ds[c_pidx[p][q]]; }
 // volume coefficient of letters (0-based vertices; -1 = absent)
 __device__ __forceinline__ double v4(const double* vt, int a, int b, int c, int d) {
     return vt[(((a + 1) * 5 + (b + 1)) * 5 + (c + 1)) * 5 + (d + 1)];
@@ -106,7 +127,8 @@ __device__ __forceinline__ void face_verts(uint64_t m, int f, int& a, int& b, in
 }
 
 // Edge x edge block (fem/mth/tet.py:887-939).
-__device__ void block_ee(const TetRec& r, const double* vt, int e, int j, double D[2][2], double F[2][2]) {
+template <class Rec>
+__device__ void block_ee(const Rec& r, const double* vt, int e, int j, double D[2][2], double F[2][2]) {
     int A, B, C, Dl;
     edge_verts(r.lmap, e, A, B);
     edge_verts(r.lmap, j, C, Dl);
@@ -124,7 +146,8 @@ __device__ void block_ee(const TetRec& r, const double* vt, int e, int j, double
 }
 
 // Edge (rows) x face (columns) block (fem/mth/tet.py:941-993).
-__device__ void block_ef(const TetRec& r, const double* vt, int e, int f, double D[2][2], double F[2][2]) {
+template <class Rec>
+__device__ void block_ef(const Rec& r, const double* vt, int e, int f, double D[2][2], double F[2][2]) {
     int A, B, C, Dl, Fl;
     edge_verts(r.lmap, e, A, B);
     face_verts(r.lmap, f, C, Dl, Fl);
@@ -146,7 +169,8 @@ __device__ void block_ef(const TetRec& r, const double* vt, int e, int f, double
 
 // Face x face block (fem/mth/tet.py:1006-1083), including the reference's
 // choice of coefficient letters in the asymmetric mass terms.
-__device__ void block_ff(const TetRec& r, const double* vt, int fi, int fj, double D[2][2], double F[2][2]) {
+template <class Rec>
+__device__ void block_ff(const Rec& r, const double* vt, int fi, int fj, double D[2][2], double F[2][2]) {
     int A, B, E, C, Dl, Fl;
     face_verts(r.lmap, fi, A, B, E);
     face_verts(r.lmap, fj, C, Dl, Fl);
@@ -177,7 +201,8 @@ __device__ void block_ff(const TetRec& r, const double* vt, int fi, int fj, doub
 
 // Block (row entity slot s, column entity slot j) of a tet, geometric part
 // (without the material scale and without kd / kf).
-__device__ __forceinline__ void tet_block(const TetRec& r, const double* vt, int s, int j, double D[2][2],
+template <class Rec>
+__device__ __forceinline__ void tet_block(const Rec& r, const double* vt, int s, int j, double D[2][2],
                                           double F[2][2]) {
     if (s < 6) {
         if (j < 6) block_ee(r, vt, s, j, D, F);
@@ -341,6 +366,8 @@ __global__ void k_tet_prep(const double* __restrict__ nodes, int64_t nN, const i
             G[i][0] = sb; G[i][1] = sc; G[i][2] = sd;
         }
         TetRec r;
+        for (int i = 0; i < 4; ++i)
+            for (int k = 0; k < 3; ++k) r.G[i * 3 + k] = G[i][k];
         for (int p = 0; p < 4; ++p)
             for (int q = p; q < 4; ++q) r.gram[c_gidx[p][q]] = G[p][0] * G[q][0] + G[p][1] * G[q][1] + G[p][2] * G[q][2];
         double X[6][3];
@@ -464,6 +491,119 @@ __global__ void __launch_bounds__(32 * kFillWarps) k_fill(const TetRec* __restri
     }
 }
 
+// Tensor materials (the reference's full (3,3) er / matinv(ur) per tet): thread per
+// tet, invariants in the reference's evaluation order (matmul(M, v) row by row, then
+// dot_c; fem/mth/tet.py:35-40,918-925,967-982), with no fused multiply-add.  The
+// imaginary part of G and X is zero, so every complex product splits into a real
+// and an imaginary evaluation of the same real expression.
+__global__ void k_tensor_prep(const TetRec* __restrict__ recs, int64_t nT, const double2* __restrict__ eps9,
+                              const double2* __restrict__ muinv9, double* __restrict__ tinv) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nT; t += (int64_t)gridDim.x * blockDim.x) {
+        double G[4][3];
+        for (int i = 0; i < 12; ++i) G[i / 3][i % 3] = recs[t].G[i];
+        double X[6][3];
+        const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
+        for (int P = 0; P < 6; ++P) {
+            const double* u = G[pa[P]];
+            const double* v = G[pb[P]];
+            X[P][0] = __dsub_rn(__dmul_rn(u[1], v[2]), __dmul_rn(u[2], v[1]));
+            X[P][1] = __dsub_rn(__dmul_rn(u[2], v[0]), __dmul_rn(u[0], v[2]));
+            X[P][2] = __dsub_rn(__dmul_rn(u[0], v[1]), __dmul_rn(u[1], v[0]));
+        }
+        double* out = tinv + t * (2 * kTInv);
+        for (int part = 0; part < 2; ++part) {
+            double Mm[9], Ms[9];
+            for (int i = 0; i < 9; ++i) {
+                const double2 a = eps9[i * nT + t], b = muinv9[i * nT + t];
+                Mm[i] = part ? a.y : a.x;
+                Ms[i] = part ? b.y : b.x;
+            }
+            double* o = out + part * kTInv;
+            for (int q = 0; q < 4; ++q) {
+                double w[3];
+                for (int k = 0; k < 3; ++k)
+                    w[k] = __dadd_rn(__dadd_rn(__dmul_rn(Mm[3 * k], G[q][0]), __dmul_rn(Mm[3 * k + 1], G[q][1])),
+                                     __dmul_rn(Mm[3 * k + 2], G[q][2]));
+                for (int p = 0; p < 4; ++p)
+                    o[p * 4 + q] = __dadd_rn(__dadd_rn(__dmul_rn(G[p][0], w[0]), __dmul_rn(G[p][1], w[1])),
+                                             __dmul_rn(G[p][2], w[2]));
+            }
+            for (int R = 0; R < 6; ++R) {
+                double w[3];
+                for (int k = 0; k < 3; ++k)
+                    w[k] = __dadd_rn(__dadd_rn(__dmul_rn(Ms[3 * k], X[R][0]), __dmul_rn(Ms[3 * k + 1], X[R][1])),
+                                     __dmul_rn(Ms[3 * k + 2], X[R][2]));
+                for (int P = 0; P < 6; ++P)
+                    o[16 + P * 6 + R] = __dadd_rn(__dadd_rn(__dmul_rn(X[P][0], w[0]), __dmul_rn(X[P][1], w[1])),
+                                                  __dmul_rn(X[P][2], w[2]));
+            }
+        }
+    }
+}
+
+// Entity-owner FP64 fill for tensor materials: as k_fill, with the block formulas
+// evaluated once on the real and once on the imaginary invariants (both are linear
+// in them) and scaled by the geometric factors only.
+__global__ void __launch_bounds__(32 * kFillWarps) k_fill_tensor(const TetRec* __restrict__ recs,
+                                                                  const double* __restrict__ tinv,
+                                                                  const int32_t* ent_list, int64_t n_ent,
+                                                                  const int32_t* __restrict__ partner,
+                                                                  const int64_t* __restrict__ inc_ptr,
+                                                                  const int64_t* __restrict__ inc,
+                                                                  const int64_t* __restrict__ indptr,
+                                                                  const int32_t* __restrict__ indices, double2* E,
+                                                                  double2* B) {
+    __shared__ double vt[625];
+    for (int i = threadIdx.x; i < 625; i += blockDim.x) vt[i] = c_vcoef[i];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t e = blockIdx.x * (int64_t)kFillWarps + w; e < n_ent; e += (int64_t)gridDim.x * kFillWarps) {
+        const int32_t r1 = ent_list[e];
+        const int32_t r2 = partner[r1];
+        const int64_t b1 = indptr[r1], b2 = indptr[r2];
+        const int n = (int)(indptr[r1 + 1] - b1);
+        for (int c = lane; c < n; c += 32) {
+            E[b1 + c] = make_double2(0.0, 0.0);
+            E[b2 + c] = make_double2(0.0, 0.0);
+            B[b1 + c] = make_double2(0.0, 0.0);
+            B[b2 + c] = make_double2(0.0, 0.0);
+        }
+        __syncwarp();
+        const int32_t* cols = indices + b1;
+        const int64_t i0 = inc_ptr[r1], i1 = inc_ptr[r1 + 1];
+        for (int64_t i = i0; i < i1; ++i) {
+            const int64_t code = inc[i];
+            const int64_t t = code >> 4;
+            const int s = (int)(code & 15);
+            if (lane < 10) {
+                const TetRec& r = recs[t];
+                const TView vre{r.len, r.ds, r.lmap, tinv + t * (2 * kTInv)};
+                const TView vim{r.len, r.ds, r.lmap, tinv + t * (2 * kTInv) + kTInv};
+                double Dr[2][2], Fr[2][2], Di[2][2], Fi[2][2];
+                tet_block(vre, vt, s, lane, Dr, Fr);
+                tet_block(vim, vt, s, lane, Di, Fi);
+                const double kd = r.kd, kf = r.kf;
+                const int p[2] = {find_col(cols, n, r.dof[lane]), find_col(cols, n, r.dof[lane + 10])};
+                const int64_t rb[2] = {b1, b2};
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) {
+                        const int64_t o = rb[a] + p[b];
+                        double2 ve = E[o], vb = B[o];
+                        ve.x += kd * Dr[a][b];
+                        ve.y += kd * Di[a][b];
+                        vb.x += kf * Fr[a][b];
+                        vb.y += kf * Fi[a][b];
+                        E[o] = ve;
+                        B[o] = vb;
+                    }
+            }
+            __syncwarp();
+        }
+    }
+}
+
 }  // namespace
 }  // namespace emg
 
@@ -481,6 +621,9 @@ struct emg_plan {
     double* mu_dev = nullptr;
     double* E_dev = nullptr;
     double* B_dev = nullptr;
+    double* tinv = nullptr;        // tensor-material invariants (2 x 52 per tet), on first use
+    double* eps9_dev = nullptr;    // staging for the tensor host entry point
+    double* mu9_dev = nullptr;
     emg::DfPlan df;                // float-float fast fill (emg_fill_df.cu)
 };
 
@@ -500,6 +643,9 @@ void free_plan(emg_plan* p) {
     emg::dfree(p->mu_dev);
     emg::dfree(p->E_dev);
     emg::dfree(p->B_dev);
+    emg::dfree(p->tinv);
+    emg::dfree(p->eps9_dev);
+    emg::dfree(p->mu9_dev);
     delete p;
 }
 
@@ -635,8 +781,8 @@ extern "C" int emg_plan_create(int64_t n_nodes, int64_t n_tets, int64_t n_edges,
     // fast fill: float-float blocks for entities within its limits
     TRY(df_plan_build(nodes, n_nodes, tets, n_tets, edges, n_edges, tris, n_tris, tet_to_field, tet_to_edge,
                       edge_lengths, p->ent_list, p->n_ent, p->inc_ptr, p->inc, p->indptr, &p->df, s));
-    // FP64 fill records only when some entity is outside the fast-fill limits
-    if (p->df.n_slow > 0) {
+    // FP64 records: the fill of entities outside the fast-fill limits and of tensor materials
+    if (n_tets > 0) {
         TRY(dalloc(&p->recs, n_tets, "tet records"));
         k_tet_prep<<<grid_for(n_tets, T), T, 0, s>>>(nodes, n_nodes, tets, n_tets, edges, n_edges, tris, n_tris,
                                                      tet_to_field, tet_to_edge, edge_lengths, p->recs, d_err);
@@ -688,12 +834,12 @@ extern "C" int emg_assemble_tet_host(emg_plan* p, const double* eps, const doubl
     EMG_CHECK_ARG(p != nullptr, "emg_assemble_tet_host: NULL plan");
     EMG_CHECK_ARG(p->nnz == 0 || (eps && mu_inv && E_data && B_data), "emg_assemble_tet_host: NULL array");
     cudaStream_t s = (cudaStream_t)stream;
-    if (!p->eps_dev) {
+    {
         int rc;
-        if ((rc = dalloc(&p->eps_dev, 2 * p->nT, "eps staging"))) return rc;
-        if ((rc = dalloc(&p->mu_dev, 2 * p->nT, "mu staging"))) return rc;
-        if ((rc = dalloc(&p->E_dev, 2 * p->nnz, "E staging"))) return rc;
-        if ((rc = dalloc(&p->B_dev, 2 * p->nnz, "B staging"))) return rc;
+        if (!p->eps_dev && (rc = dalloc(&p->eps_dev, 2 * p->nT, "eps staging"))) return rc;
+        if (!p->mu_dev && (rc = dalloc(&p->mu_dev, 2 * p->nT, "mu staging"))) return rc;
+        if (!p->E_dev && (rc = dalloc(&p->E_dev, 2 * p->nnz, "E staging"))) return rc;
+        if (!p->B_dev && (rc = dalloc(&p->B_dev, 2 * p->nnz, "B staging"))) return rc;
     }
     if (p->nT > 0) {
         EMG_CUDA(cudaMemcpyAsync(p->eps_dev, eps, sizeof(double) * 2 * p->nT, cudaMemcpyHostToDevice, s));
@@ -701,6 +847,52 @@ extern "C" int emg_assemble_tet_host(emg_plan* p, const double* eps, const doubl
     }
     int rc = emg_assemble_tet(p, p->eps_dev, p->mu_dev, p->E_dev, p->B_dev, stream);
     if (rc) return rc;
+    if (p->nnz > 0) {
+        EMG_CUDA(cudaMemcpyAsync(E_data, p->E_dev, sizeof(double) * 2 * p->nnz, cudaMemcpyDeviceToHost, s));
+        EMG_CUDA(cudaMemcpyAsync(B_data, p->B_dev, sizeof(double) * 2 * p->nnz, cudaMemcpyDeviceToHost, s));
+    }
+    EMG_CUDA(cudaStreamSynchronize(s));
+    return EMG_OK;
+}
+
+extern "C" int emg_assemble_tet_tensor(emg_plan* p, const double* eps9, const double* mu_inv9, double* E_data,
+                                       double* B_data, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p != nullptr, "emg_assemble_tet_tensor: NULL plan");
+    EMG_CHECK_ARG(p->nnz == 0 || (eps9 && mu_inv9 && E_data && B_data), "emg_assemble_tet_tensor: NULL array");
+    if (p->n_ent == 0) return EMG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!p->tinv) {
+        int rc = dalloc(&p->tinv, p->nT * 2 * kTInv, "tensor invariants");
+        if (rc) return rc;
+    }
+    k_tensor_prep<<<grid_for(p->nT, 128), 128, 0, s>>>(p->recs, p->nT, reinterpret_cast<const double2*>(eps9),
+                                                       reinterpret_cast<const double2*>(mu_inv9), p->tinv);
+    EMG_CUDA(cudaGetLastError());
+    const unsigned g = grid_for(p->n_ent, kFillWarps, 152u * 16u);
+    k_fill_tensor<<<g, 32 * kFillWarps, 0, s>>>(p->recs, p->tinv, p->ent_list, p->n_ent, p->partner, p->inc_ptr,
+                                                p->inc, p->indptr, p->indices, reinterpret_cast<double2*>(E_data),
+                                                reinterpret_cast<double2*>(B_data));
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+
+extern "C" int emg_assemble_tet_tensor_host(emg_plan* p, const double* eps9, const double* mu_inv9, double* E_data,
+                                            double* B_data, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(p != nullptr, "emg_assemble_tet_tensor_host: NULL plan");
+    EMG_CHECK_ARG(p->nnz == 0 || (eps9 && mu_inv9 && E_data && B_data), "emg_assemble_tet_tensor_host: NULL array");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc;
+    if (!p->eps9_dev && (rc = dalloc(&p->eps9_dev, 18 * p->nT, "eps tensor staging"))) return rc;
+    if (!p->mu9_dev && (rc = dalloc(&p->mu9_dev, 18 * p->nT, "mu tensor staging"))) return rc;
+    if (!p->E_dev && (rc = dalloc(&p->E_dev, 2 * p->nnz, "E staging"))) return rc;
+    if (!p->B_dev && (rc = dalloc(&p->B_dev, 2 * p->nnz, "B staging"))) return rc;
+    if (p->nT > 0) {
+        EMG_CUDA(cudaMemcpyAsync(p->eps9_dev, eps9, sizeof(double) * 18 * p->nT, cudaMemcpyHostToDevice, s));
+        EMG_CUDA(cudaMemcpyAsync(p->mu9_dev, mu_inv9, sizeof(double) * 18 * p->nT, cudaMemcpyHostToDevice, s));
+    }
+    if ((rc = emg_assemble_tet_tensor(p, p->eps9_dev, p->mu9_dev, p->E_dev, p->B_dev, stream))) return rc;
     if (p->nnz > 0) {
         EMG_CUDA(cudaMemcpyAsync(E_data, p->E_dev, sizeof(double) * 2 * p->nnz, cudaMemcpyDeviceToHost, s));
         EMG_CUDA(cudaMemcpyAsync(B_data, p->B_dev, sizeof(double) * 2 * p->nnz, cudaMemcpyDeviceToHost, s));

@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .assembly import AssemblyPlan, material_scalars, plan_for
+from .assembly import AssemblyPlan, plan_for
 from .bc import C0, is_pec, is_robin
 
 # Dunavant order-4 rule (6 points) as weights and barycentrics, the rule
@@ -126,8 +126,7 @@ class Assembler:
         key = id(field)
         if self._dev is None or self._dev[0] != key:
             plan = plan_for(field, self.device)
-            eps, mu_inv = material_scalars(er, ur)
-            E, B = plan.assemble(torch.as_tensor(eps, device=self.device), torch.as_tensor(mu_inv, device=self.device))
+            E, B = plan.assemble_materials(er, ur)
             self._dev = (key, plan, E, B)
         return self._dev[1], self._dev[2], self._dev[3]
 

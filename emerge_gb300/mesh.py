@@ -54,18 +54,23 @@ class TetMesh:
         tets: (4, nT) int64 vertex indices per tetrahedron.
         boundary: optional {face_tag: (3, n) int64 triangle vertex indices}.
         cell_tag: optional (nT,) int64 tag per tet (material/volume id).
+        device: build the topology on this CUDA device (``topology.build_topology``)
+            instead of with NumPy on the host; the arrays are the same.
     """
 
     def __init__(self, nodes: np.ndarray, tets: np.ndarray,
                  boundary: dict[int, np.ndarray] | None = None,
-                 cell_tag: np.ndarray | None = None):
+                 cell_tag: np.ndarray | None = None, device=None):
         self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
         self.tets = np.ascontiguousarray(tets, dtype=np.int64)
         self.boundary = {} if boundary is None else {int(k): np.asarray(v, dtype=np.int64)
                                                       for k, v in boundary.items()}
         nT = self.tets.shape[1]
         self.cell_tag = np.zeros(nT, dtype=np.int64) if cell_tag is None else np.asarray(cell_tag, dtype=np.int64)
-        self._build()
+        if device is None:
+            self._build()
+        else:
+            self._build_device(device)
 
     # -- sizes (Mesh3D properties, fem/mesh3d.py:118-136)
     @property
@@ -134,6 +139,18 @@ class TetMesh:
         self.centers = self.nodes[:, T].mean(axis=1)
         self._ufk = ufk
 
+    def _build_device(self, device) -> None:
+        from .topology import build_topology
+        t = build_topology(self.nodes, self.tets, device)
+        self.edges, self.tris = t["edges"], t["tris"]
+        self.tet_to_edge, self.tet_to_tri = t["tet_to_edge"], t["tet_to_tri"]
+        self.tri_to_edge, self.tri_to_tet = t["tri_to_edge"], t["tri_to_tet"]
+        self.edge_lengths = t["edge_lengths"]
+        self.tet_to_field = t["tet_to_field"]
+        self.centers = self.nodes[:, self.tets].mean(axis=1)
+        nN = self.n_nodes
+        self._ufk = (self.tris[0] * nN + self.tris[1]) * nN + self.tris[2] if nN < (1 << 21) else None
+
     def get_edge(self, i1: int, i2: int) -> int:
         lo, hi = min(i1, i2), max(i1, i2)
         k = lo * self.n_nodes + hi
@@ -142,6 +159,8 @@ class TetMesh:
 
     def tri_ids(self, tri_vertices: np.ndarray) -> np.ndarray:
         """Indices of the faces with the given (3, n) vertex triples (any order)."""
+        if self._ufk is None:
+            raise ValueError("face lookup by vertex triple supports up to 2**21 vertices")
         s = np.sort(np.asarray(tri_vertices, dtype=np.int64), axis=0)
         key = _pack([s[0], s[1], s[2]], self.n_nodes)
         idx = np.searchsorted(self._ufk, key)

@@ -77,6 +77,21 @@ int emg_assemble_tet(emg_plan* plan, const double* eps, const double* mu_inv, do
 int emg_assemble_tet_host(emg_plan* plan, const double* eps, const double* mu_inv, double* E_data,
                           double* B_data, void* stream);
 
+/* Tensor (anisotropic) materials: the general case of _matrix_builder
+ * (fem/physics/edm/optimized_assembly.py:66-116), which passes the (3,3)
+ * tensors er[:,:,t] and matinv(ur[:,:,t]) (fem/mth/optimized.py:441-461) to
+ * ned2_tet_stiff_mass as Mm and Ms.
+ *   eps9, mu_inv9: complex (9, n_tets), element (i, j) of tet t at
+ *     (i*3 + j)*n_tets + t, i.e. the reference's (3,3,nT) array in C order;
+ *     mu_inv9 already holds matinv(ur) per tet.
+ * FP64 on the CUDA cores (warp per DOF entity, as emg_assemble_tet); same
+ * pattern, same output layout.  Device arrays; the _host variant takes host
+ * arrays, copies them around the call and synchronises ``stream``. */
+int emg_assemble_tet_tensor(emg_plan* plan, const double* eps9, const double* mu_inv9, double* E_data,
+                            double* B_data, void* stream);
+int emg_assemble_tet_tensor_host(emg_plan* plan, const double* eps9, const double* mu_inv9, double* E_data,
+                                 double* B_data, void* stream);
+
 /* Releases the plan and its device memory. */
 void emg_plan_destroy(emg_plan* plan);
 
@@ -314,6 +329,31 @@ void emg_mlp_destroy(emg_mlp* mlp);
  * Synchronises ``stream``. */
 int emg_csr_pattern_noalloc(int64_t n_tets, int64_t n_field, const int32_t* tet_to_field, int64_t* indptr,
                             int32_t* indices, int64_t indices_capacity, int64_t* nnz_out, void* stream);
+
+/* ------------------------------------------------------- mesh topology ---
+ * Replace the topology loops of Mesh3D.update (fem/mesh3d.py:224-355) and the
+ * DOF map of Nedelec2.__init__ (fem/elements/nedelec2.py:32-62): edges and
+ * faces of a tetrahedral mesh numbered in ascending vertex-tuple order, the
+ * tet -> edge / face maps in the reference's slot order, tri -> edge, tri ->
+ * tet and tet_to_field.  tets: DEVICE (4, n_tets) int32.  Synchronises
+ * ``stream``; EMG_ERR_MESH for a vertex index out of range or a face shared by
+ * more than two tets. */
+typedef struct emg_topology emg_topology;
+int emg_topology_create(int64_t n_nodes, int64_t n_tets, const int32_t* tets, void* stream, emg_topology** out);
+int emg_topology_sizes(const emg_topology* topo, int64_t* n_edges, int64_t* n_tris);
+/* Copies into caller-owned DEVICE arrays (int32; any may be NULL to skip it):
+ * edges (2, nE), tris (3, nTri), tet_to_edge (6, nT), tet_to_tri (4, nT),
+ * tri_to_edge (3, nTri), tri_to_tet (2, nTri; -1 = no second tet),
+ * tet_to_field (20, nT). */
+int emg_topology_get(const emg_topology* topo, int32_t* edges, int32_t* tris, int32_t* tet_to_edge,
+                     int32_t* tet_to_tri, int32_t* tri_to_edge, int32_t* tri_to_tet, int32_t* tet_to_field,
+                     void* stream);
+void emg_topology_destroy(emg_topology* topo);
+/* Edge lengths sqrt(dx^2 + dy^2 + dz^2) (fem/mesh3d.py:351), each step rounded
+ * in order (bitwise equal to NumPy's).  nodes (3, n_nodes) f64, edges (2,
+ * n_edges) int32, lengths (n_edges) f64: DEVICE arrays. */
+int emg_edge_lengths(int64_t n_nodes, const double* nodes, int64_t n_edges, const int32_t* edges, double* lengths,
+                     void* stream);
 
 #ifdef __cplusplus
 }

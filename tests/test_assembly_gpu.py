@@ -125,14 +125,61 @@ def test_bad_mesh_is_rejected(torch_cuda):
         AssemblyPlan(field)
 
 
-def test_anisotropic_material_is_rejected(torch_cuda):
+def _random_tensors(nT, seed):
+    """Full complex (3,3,nT) tensors: lossy, non-symmetric, diagonally dominant."""
+    rng = np.random.default_rng(seed)
+    er = (rng.uniform(-0.8, 0.8, (3, 3, nT)) + 1j * rng.uniform(-0.05, 0.05, (3, 3, nT)))
+    ur = (rng.uniform(-0.3, 0.3, (3, 3, nT)) + 1j * rng.uniform(-0.02, 0.02, (3, 3, nT)))
+    for k in range(3):
+        er[k, k] += rng.uniform(2, 10, nT) * (1 - 1j * rng.uniform(0.001, 0.02, nT))
+        ur[k, k] += rng.uniform(0.8, 3, nT)
+    return er, ur
+
+
+@pytest.mark.parametrize("n,kind", [(5, "full"), (7, "diagonal"), (6, "mixed")])
+def test_tensor_materials_match_oracle(torch_cuda, n, kind):
+    """Anisotropic er / ur (the general _matrix_builder case) through the tensor fill."""
     from emerge_gb300.assembly import tet_mass_stiffness_matrices
-    z = load("small_assembly.npz")
-    field = field_from(z)
-    er = z["er_a"].copy()
-    er[0, 1, 0] = 0.1
-    with pytest.raises(NotImplementedError):
-        tet_mass_stiffness_matrices(field, er, z["ur_a"])
+    from emerge_gb300.mesh import Nedelec2Basis, unit_cube
+    m = unit_cube(n, jitter=0.15, seed=n)
+    field = Nedelec2Basis(m)
+    er, ur = _random_tensors(m.n_tets, 40 + n)
+    if kind == "diagonal":           # diag(a, b, c): matinv's reciprocal branch
+        er = er * np.eye(3)[:, :, None]
+        ur = ur * np.eye(3)[:, :, None]
+    elif kind == "mixed":            # isotropic tets next to full tensors
+        iso_er, iso_ur = _random_materials(m.n_tets, n, mu_one=False)
+        pick = np.arange(m.n_tets) % 3 == 0
+        er[:, :, pick] = iso_er[:, :, pick]
+        ur[:, :, pick] = iso_ur[:, :, pick]
+    E, B = tet_mass_stiffness_matrices(field, er, ur)
+    Eo, Bo = oracle.tet_mass_stiffness_matrices(field, er, ur)
+    assert rel_to_rowmax(E, Eo) <= TOL
+    assert rel_to_rowmax(B, Bo) <= TOL
+
+
+def test_tensor_fill_of_isotropic_tensors_matches_scalar_fill(torch_cuda):
+    """The tensor fill given s·I tensors agrees with the float-float scalar fill."""
+    torch = torch_cuda
+    from emerge_gb300.assembly import AssemblyPlan, material_scalars, matinv_tensors
+    from emerge_gb300.mesh import Nedelec2Basis, unit_cube
+    m = unit_cube(6, jitter=0.15, seed=3)
+    field = Nedelec2Basis(m)
+    er, ur = _random_materials(m.n_tets, 8, mu_one=False)
+    plan = AssemblyPlan(field)
+    eps, mu_inv = material_scalars(er, ur)
+    E1, B1 = plan.assemble(torch.as_tensor(eps, device="cuda"), torch.as_tensor(mu_inv, device="cuda"))
+    E2, B2 = plan.assemble_tensor(torch.as_tensor(er.reshape(9, -1).copy(), device="cuda"),
+                                  torch.as_tensor(matinv_tensors(ur).reshape(9, -1).copy(), device="cuda"))
+    Eh, Bh = plan.assemble_tensor_host(er.reshape(9, -1), matinv_tensors(ur).reshape(9, -1))
+    torch.cuda.synchronize()
+    ip, ix = plan.pattern_host()
+    from scipy.sparse import csr_matrix
+    N = plan.n_field
+    mk = lambda v: csr_matrix((v, ix, ip), shape=(N, N))  # noqa: E731
+    assert rel_to_rowmax(mk(E2.cpu().numpy()), mk(E1.cpu().numpy())) <= TOL
+    assert rel_to_rowmax(mk(B2.cpu().numpy()), mk(B1.cpu().numpy())) <= TOL
+    assert np.array_equal(Eh, E2.cpu().numpy()) and np.array_equal(Bh, B2.cpu().numpy())
 
 
 def test_high_valence_edge_matches_oracle(torch_cuda):
