@@ -170,6 +170,12 @@ def run_reference(args, rank, world):
     }))
 
 
+# FP64 flops per tet of the factored isotropic element blocks plus the complex
+# material scaling and accumulation (36 ee x 40 + 48 ef/fe x 73 + 16 ff x 129 + 100 x 36)
+FILL_FLOPS_PER_TET = 10608
+FP64_TFLOPS = 1.18      # GB300 DFMA throughput measured by a probe kernel
+
+
 def run_gpu(args, rank, world):
     import torch
     from emerge_gb300 import _build
@@ -256,10 +262,17 @@ def run_gpu(args, rank, world):
                 "d2h_bytes_per_step": int(2 * 16 * nnz), "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "kernel": "k_scales + k_fill_df (one assembly step)",
-                     "algorithmic_bytes_per_launch": int(alg_bytes), "traffic": traffic_per_launch(n)},
+                     "algorithmic_bytes_per_launch": int(alg_bytes), "traffic": traffic_per_launch(n),
+                     # the element arithmetic: FP64 flops of the factored isotropic block formulas
+                     # per tet (counted from the FP64 fill's formulas) at GB300's measured DFMA rate
+                     "compute": {"bound": "fp64-equivalent", "flops_per_tet": FILL_FLOPS_PER_TET,
+                                 "peak_tflops": FP64_TFLOPS, "floor_ms": FILL_FLOPS_PER_TET * nT / FP64_TFLOPS / 1e9,
+                                 "frac": FILL_FLOPS_PER_TET * nT / FP64_TFLOPS / 1e9 / statistics.median(launch_ms)}},
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
+    if rank == 0:
+        out["topology"] = run_topology(m, n, dev)
     if rank == 0 and not args.no_sweep:
         del E, B, pin_E, pin_B, npE, npB, plan
         torch.cuda.empty_cache()
@@ -276,21 +289,52 @@ def run_gpu(args, rank, world):
         print(json.dumps(out))
 
 
+def run_topology(m, n, dev):
+    """Mesh topology + DOF map of the same mesh: GPU sort build vs the NumPy host build.
+
+    ``gpu_s``: host arrays in, host int64 arrays out (copies included);
+    ``gpu_device_s``: device-resident tets / nodes in, device arrays out."""
+    import torch
+    from emerge_gb300.mesh import TetMesh
+    from emerge_gb300.topology import build_topology
+    build_topology(m.nodes, m.tets[:, :6000], dev)          # warm-up (library, sort temp sizes)
+    nodes_d = torch.as_tensor(m.nodes, device=dev)
+    tets_d = torch.as_tensor(m.tets.astype(np.int32), device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    build_topology(nodes_d, tets_d, dev, keep_on_device=True)
+    torch.cuda.synchronize()
+    t_dev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    d = build_topology(m.nodes, m.tets, dev)
+    t_gpu = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    h = TetMesh(m.nodes, m.tets)
+    t_host = time.perf_counter() - t0
+    same = all(np.array_equal(getattr(h, k), d[k]) for k in ("edges", "tris", "tet_to_edge", "tet_to_tri",
+                                                             "tri_to_edge", "tri_to_tet", "edge_lengths"))
+    return {"workload": f"{n}^3 Kuhn cube: {m.n_tets} tets -> {h.n_edges} edges, {h.n_tris} faces",
+            "gpu_device_s": round(t_dev, 4), "gpu_s": round(t_gpu, 4), "host_numpy_s": round(t_host, 3),
+            "identical_to_host": bool(same)}
+
+
 def run_sweep(args):
-    """Iris-filter sweep: batched + mixed-precision + MLP-warm-started vs the plain FP64 GPU solve.
+    """Iris-filter sweep: batched + mixed-precision + warm-started vs the plain FP64 GPU solve.
 
     freq-pts/s = points / wall time of the solve phase (volume and port matrices
-    assembled before; both methods form A(k) themselves).
+    assembled before; every method forms A(k) itself and pays its own factorizations).
       plain  — one frequency at a time: slab factorization of A(k) in complex FP64 +
                FGMRES (a direct solve: 1-2 iterations), both ports together; timed
                on ``--sweep-plain`` points spread over the band, rate extrapolated.
       fast   — all points: FP32 slab factors at ``--sweep-anchors`` anchor
-               frequencies (one batched factorization), the first ``--sweep-train``
-               points solved by batched FGMRES, the BF16 tensor-core MLP trained on
-               them supplies every point's initial guess, then batched FGMRES on all
-               columns to the same FP64 residual tolerance.
-    max|dS| compares fast with plain on the plain points.  Also reported: the same
-    anchored sweep without a warm start (what the learned guess saves), the
+               frequencies (one batched factorization), ``--sweep-train`` points spread
+               over the band solved by batched FGMRES, the minimal-residual projection
+               onto their span as every other point's initial guess, then batched
+               FGMRES on those columns to the same FP64 residual tolerance.
+      mlp    — the same with the BF16 tensor-core MLP (trained on ``--sweep-mlp-train``
+               points) supplying the initial guesses instead of the projection.
+      cold   — the same anchored batched FGMRES from zero initial guesses.
+    max|dS| compares each with plain on the plain points.  Also reported: the
     ILU(0)-GMRES plain method on one point with capped iterations, and SciPy's
     SuperLU (the reference's default direct solver) per point on the host cores.
     """
@@ -320,42 +364,49 @@ def run_sweep(args):
     # the slab products' layout, tuned once per mesh and column pattern (not timed)
     out["autotune"] = sw.autotune(freqs, n_anchor=args.sweep_anchors, chunk=chunk)
     out["autotune"]["seconds"] = round(out["autotune"]["seconds"], 2)
+    kw = dict(precision="fp32", tol=args.sweep_tol, restart=args.sweep_restart, chunk=chunk,
+              refine=args.sweep_refine, inner=args.sweep_inner)
     with ClockSampler(0) as clk:
         # warm-up of every code path on a tiny sweep (graph capture, cuBLAS/cuSOLVER handles)
-        sw.run_warm(freqs[:4], n_train=2, solver="anchored", n_anchor=1, precision="fp32", guess="mlp",
-                    tol=args.sweep_tol, mlp_steps=50)
-        sw._slab_key = None
-        kw = dict(precision="fp32", tol=args.sweep_tol, restart=args.sweep_restart, chunk=chunk,
-                  refine=args.sweep_refine, inner=args.sweep_inner)
-        fast = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored", n_anchor=args.sweep_anchors,
-                           guess="mlp", mlp_steps=args.sweep_mlp_steps, **kw)
+        # (the basis sizes of the timed runs, on every tenth frequency)
+        for guess, ntr in (("projection", args.sweep_train), ("mlp", args.sweep_mlp_train)):
+            sw.run_warm(freqs[::10], n_train=min(ntr, len(freqs[::10]) - 1), solver="anchored", n_anchor=1,
+                        precision="fp32", guess=guess, tol=args.sweep_tol, mlp_steps=50)
         # every variant pays its own anchor factorization (the factors are cached per key)
         sw._slab_key = None
-        proj = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored", n_anchor=args.sweep_anchors,
+        fast = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored", n_anchor=args.sweep_anchors,
                            guess="projection", **kw)
+        sw._slab_key = None
+        mlp = sw.run_warm(freqs, n_train=min(args.sweep_mlp_train, nf), solver="anchored",
+                          n_anchor=args.sweep_anchors, guess="mlp", mlp_steps=args.sweep_mlp_steps, **kw)
         sw._slab_key = None
         cold = sw.run_anchored(freqs, n_anchor=args.sweep_anchors, **kw)
         plain = sw.run(freqs[idx], method="plain", precond="slab64", tol=args.sweep_tol)
     v_fast = nf / fast.seconds
     v_plain = len(idx) / plain.seconds
+    pred = mlp.info["final_index"]
     out.update({
         "fast": v_fast, "plain": v_plain, "ratio": v_fast / v_plain,
         "max_abs_dS_vs_plain": float(np.max(np.abs(fast.S[idx] - plain.S))),
         "max_residual_fast": float(fast.residuals.max()), "max_residual_plain": float(plain.residuals.max()),
         "fast_seconds": round(fast.seconds, 3), "plain_seconds_per_point": round(plain.seconds / len(idx), 3),
         "plain_points_timed": int(len(idx)), "anchors": args.sweep_anchors, "precision_inner": "complex fp32",
-        "factor_seconds": round(float(fast.info.get("factor_seconds", 0.0)), 3),
+        "fast_guess": "projection", "factor_seconds": round(float(fast.info.get("factor_seconds", 0.0)), 3),
         "train_points": int(fast.info["train_points"]), "train_seconds": round(fast.info["train_seconds"], 3),
-        "mlp_seconds": round(fast.info["guess_seconds"], 3), "mlp_loss": fast.info["mlp_loss"],
-        "final_seconds": round(fast.info["final_seconds"], 3),
+        "guess_seconds": round(fast.info["guess_seconds"], 3), "final_seconds": round(fast.info["final_seconds"], 3),
         "iterations_fast_mean": float(fast.iterations.mean()), "iterations_fast_max": int(fast.iterations.max()),
-        # iterations on the points the warm start predicts (all but the training points)
-        "iterations_warm_predicted_mean": fast.info["final_iterations_mean"],
-        "iterations_cold_same_points_mean": float(cold.iterations[fast.info["final_index"]].mean()),
-        "iterations_cold_mean": float(cold.iterations.mean()), "cold_pts_per_s": nf / cold.seconds,
-        "max_abs_dS_cold_vs_fast": float(np.max(np.abs(cold.S - fast.S))),
-        "projection_pts_per_s": nf / proj.seconds, "iterations_projection_mean": float(proj.iterations.mean()),
-        "max_abs_dS_projection_vs_plain": float(np.max(np.abs(proj.S[idx] - plain.S))),
+        "iterations_fast_predicted_mean": fast.info["final_iterations_mean"],
+        "mlp": {"pts_per_s": nf / mlp.seconds, "seconds": round(mlp.seconds, 3),
+                "train_points": int(mlp.info["train_points"]), "train_seconds": round(mlp.info["train_seconds"], 3),
+                "mlp_seconds": round(mlp.info["guess_seconds"], 3), "mlp_loss": mlp.info["mlp_loss"],
+                "final_seconds": round(mlp.info["final_seconds"], 3),
+                # iterations on the points the network predicts (all but its training points)
+                "iterations_predicted_mean": mlp.info["final_iterations_mean"],
+                "iterations_cold_same_points_mean": float(cold.iterations[pred].mean()),
+                "max_abs_dS_vs_plain": float(np.max(np.abs(mlp.S[idx] - plain.S)))},
+        "cold": {"pts_per_s": nf / cold.seconds, "seconds": round(cold.seconds, 3),
+                 "iterations_mean": float(cold.iterations.mean()), "iterations_max": int(cold.iterations.max()),
+                 "max_abs_dS_vs_fast": float(np.max(np.abs(cold.S - fast.S)))},
         "inner": args.sweep_inner, "refine": args.sweep_refine,
         "refinement_steps": int(fast.info.get("refinement_steps", 0)),
         "iterations_plain_mean": float(plain.iterations.mean()),
@@ -469,11 +520,12 @@ def main():
     ap.add_argument("--no-sweep", action="store_true", help="skip the frequency-sweep measurement")
     ap.add_argument("--sweep-h", type=float, default=2e-3, help="iris-filter mesh size (m)")
     ap.add_argument("--sweep-points", type=int, default=401)
-    ap.add_argument("--sweep-train", type=int, default=32)
-    ap.add_argument("--sweep-anchors", type=int, default=8)
+    ap.add_argument("--sweep-train", type=int, default=16, help="points solved first; their span gives the guesses")
+    ap.add_argument("--sweep-mlp-train", type=int, default=32, help="training points of the MLP variant")
+    ap.add_argument("--sweep-anchors", type=int, default=4)
     ap.add_argument("--sweep-restart", type=int, default=40)
     ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: as many as fit ~80 GB)")
-    ap.add_argument("--sweep-mlp-steps", type=int, default=1000)
+    ap.add_argument("--sweep-mlp-steps", type=int, default=300)
     ap.add_argument("--sweep-inner", default="fp64", choices=["fp32", "fp64"],
                     help="precision of the Krylov vectors of the fast sweep (its factors are FP32 either way)")
     ap.add_argument("--sweep-refine", type=int, default=0, help="Newton-Schulz step on the FP32 slab inverses")

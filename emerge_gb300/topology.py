@@ -31,8 +31,8 @@ def build_topology(nodes: np.ndarray, tets: np.ndarray, device: str | torch.devi
     """Edges, faces, incidence maps, tet_to_field and edge lengths of a tet mesh.
 
     Args:
-        nodes: (3, nN) float64 vertex coordinates.
-        tets: (4, nT) vertex indices.
+        nodes: (3, nN) float64 vertex coordinates (NumPy, or a torch tensor).
+        tets: (4, nT) vertex indices (NumPy, or a torch tensor; int32 on the device).
         keep_on_device: return torch CUDA tensors (int32 / float64) instead of
             host int64 / float64 arrays.
 
@@ -42,8 +42,14 @@ def build_topology(nodes: np.ndarray, tets: np.ndarray, device: str | torch.devi
     """
     _lib.load()
     dev = torch.device(device)
-    nodes_d = torch.as_tensor(np.ascontiguousarray(nodes, dtype=np.float64), device=dev)
-    tets_d = torch.as_tensor(np.ascontiguousarray(tets, dtype=np.int32), device=dev)
+    if isinstance(nodes, torch.Tensor):
+        nodes_d = nodes.to(device=dev, dtype=torch.float64).contiguous()
+    else:
+        nodes_d = torch.as_tensor(np.ascontiguousarray(nodes, dtype=np.float64), device=dev)
+    if isinstance(tets, torch.Tensor):
+        tets_d = tets.to(device=dev, dtype=torch.int32).contiguous()
+    else:
+        tets_d = torch.as_tensor(np.ascontiguousarray(tets, dtype=np.int32), device=dev)
     nN, nT = int(nodes_d.shape[1]), int(tets_d.shape[1])
     h = ctypes.c_void_p()
     with torch.cuda.device(dev):

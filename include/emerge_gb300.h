@@ -355,6 +355,18 @@ void emg_topology_destroy(emg_topology* topo);
 int emg_edge_lengths(int64_t n_nodes, const double* nodes, int64_t n_edges, const int32_t* edges, double* lengths,
                      void* stream);
 
+/* --------------------------------------------------------- far field ---
+ * Stratton-Chu transform, the counterpart of stratton_chu_ff
+ * (fem/physics/edm/sc.py:26-140).  Sources j < n_src at vis (3, n_src) f32 with
+ * weights wns (3, n_src) f32 (n * area / 3 summed over the surface triangles of
+ * each edge, sc.py:159-165) and fields E, H (3, n_src) complex64; sources with
+ * |E| <= 1e-3 max|E| are dropped as the reference does.  Directions: elevation
+ * theta, azimuth phi (n_dir f32), r = (cos th cos ph, cos th sin ph, sin th).
+ * Eout, Hout: (3, n_dir) complex128.  All arrays DEVICE; synchronises ``stream``. */
+int emg_stratton_chu(int64_t n_src, const float* E, const float* H, const float* vis, const float* wns,
+                     int64_t n_dir, const float* theta, const float* phi, float k0, double* Eout, double* Hout,
+                     void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,6 +46,7 @@ def _install_numba():
     nb.jit = _njit
     nb.prange = range
     anyt = _AnyType()
+    nb.typeof = anyt
     for name in ("f8", "f4", "i8", "i4", "c16", "c8", "b1", "boolean", "int64", "float64",
                  "complex128", "void", "uint8", "int32"):
         setattr(nb, name, anyt)
@@ -72,6 +73,10 @@ def _install_numba():
     npb.ProgressBar = ProgressBar
     npb.ProgressBarType = anyt
     sys.modules["numba_progress"] = npb
+    npp = types.ModuleType("numba_progress.progress")
+    npp.ProgressBarType = anyt
+    npb.progress = npp
+    sys.modules["numba_progress.progress"] = npp
 
 
 def _install_loguru():

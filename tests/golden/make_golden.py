@@ -25,6 +25,8 @@ Fixtures:
                      SuperLU field: 6-point quadrature points of the port-1 triangles
                      over the port tets (the S-parameter evaluation) and random
                      interior points over all tets
+  farfield.npz       stratton_chu (fem/physics/edm/sc.py:143-180) of a short dipole's
+                     near field sampled at the edge centres of a closed box surface
 """
 from __future__ import annotations
 
@@ -337,8 +339,75 @@ def make_interp():
                         port_E=np.stack(Ep), inner_points=inner, inner_E=np.stack(Ei), inner_tets=tsel)
 
 
+def dipole_surface(h=6e-3, half=0.03, k0=2 * np.pi * 10e9 / C0, seed=5):
+    """A closed box surface around a z-directed short dipole at the origin.
+
+    Returns (surface dict, Ein, Hin) with the surface arrays stratton_chu reads
+    (n_tris, tri_to_edge, normals (outward), areas, edge_centers) and the dipole's
+    E and H (unit current moment) at the edge centres; a few sources are scaled
+    below sc.py's 1e-3 cut-off."""
+    g = np.linspace(-half, half, int(round(2 * half / h)) + 1)
+    tm = structured_box(g, g, g)
+    tris = []
+    normals = []
+    for tag, nrm in ((pm.FACE_XMIN, (-1, 0, 0)), (pm.FACE_XMAX, (1, 0, 0)), (pm.FACE_YMIN, (0, -1, 0)),
+                     (pm.FACE_YMAX, (0, 1, 0)), (pm.FACE_ZMIN, (0, 0, -1)), (pm.FACE_ZMAX, (0, 0, 1))):
+        t = np.asarray(tm.boundary[tag], dtype=np.int64)
+        tris.append(np.sort(t, axis=0))
+        normals.append(np.repeat(np.array(nrm, dtype=float)[:, None], t.shape[1], axis=1))
+    tris = np.concatenate(tris, axis=1)
+    normals = np.concatenate(normals, axis=1)
+    pairs = np.concatenate([tris[[0, 1]], tris[[1, 2]], tris[[0, 2]]], axis=1)
+    key = pairs[0] * tm.n_nodes + pairs[1]
+    ukey, inv = np.unique(key, return_inverse=True)
+    tri_to_edge = inv.reshape(3, -1)
+    ev = np.stack([ukey // tm.n_nodes, ukey % tm.n_nodes])
+    centers = 0.5 * (tm.nodes[:, ev[0]] + tm.nodes[:, ev[1]])
+    p0, p1, p2 = tm.nodes[:, tris[0]], tm.nodes[:, tris[1]], tm.nodes[:, tris[2]]
+    areas = 0.5 * np.linalg.norm(np.cross((p1 - p0).T, (p2 - p0).T), axis=1)
+    # short z dipole of unit current moment, e^{-jkr} convention (near + far terms):
+    # H = jk g (1 + 1/(jkr)) z x r^,  E = eta g [2/r (1 + 1/(jkr)) cos(th) r^
+    #     + jk (1 + 1/(jkr) - 1/(kr)^2) (cos(th) r^ - z)],  g = e^{-jkr} / (4 pi r)
+    r = np.linalg.norm(centers, axis=0)
+    rh = centers / r
+    kr = k0 * r
+    eta = 376.73031366857
+    g0 = np.exp(-1j * kr) / (4 * np.pi * r)
+    zhat = np.array([0.0, 0.0, 1.0])[:, None]
+    cz = rh[2]
+    a1 = 1 + 1 / (1j * kr)
+    a2 = 1 + 1 / (1j * kr) - 1 / kr ** 2
+    E = eta * g0 * (2 / r * a1 * cz * rh + 1j * k0 * a2 * (cz * rh - zhat))
+    H = 1j * k0 * g0 * a1 * np.cross(zhat.T, rh.T).T
+    rng = np.random.default_rng(seed)
+    low = rng.choice(centers.shape[1], 25, replace=False)
+    E[:, low] *= 1e-4
+    H[:, low] *= 1e-4
+    surf = dict(n_tris=tris.shape[1], tri_to_edge=tri_to_edge, normals=normals, areas=areas,
+                edge_centers=centers)
+    return surf, E, H
+
+
+def make_farfield():
+    """Reference Stratton-Chu far field of the dipole surface fields."""
+    import types as _types
+    from fem.physics.edm import sc as ref_sc
+    k0 = 2 * np.pi * 10e9 / C0
+    surf, E, H = dipole_surface(k0=k0)
+    mesh = _types.SimpleNamespace(**surf)
+    th = np.linspace(-np.pi / 2, np.pi / 2, 19)
+    ph = np.linspace(0, 2 * np.pi, 36, endpoint=False)
+    TH, PH = np.meshgrid(th, ph, indexing="ij")
+    theta, phi = TH.ravel(), PH.ravel()
+    t0 = time.time()
+    Eout, Hout = ref_sc.stratton_chu(E, H, mesh, theta, phi, k0)
+    print(f"farfield: {E.shape[1]} sources x {theta.size} directions ({time.time() - t0:.1f} s)")
+    np.savez_compressed(os.path.join(HERE, "farfield.npz"), Ein=E, Hin=H, theta=theta, phi=phi, k0=k0,
+                        Eout=Eout, Hout=Hout, **surf)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc", "interp"]
+    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc", "interp", "farfield"]
     if "tet" in which:
         make_tet_elements()
     if "tri" in which:
@@ -351,3 +420,5 @@ if __name__ == "__main__":
         make_waveguide_abc()
     if "interp" in which:
         make_interp()
+    if "farfield" in which:
+        make_farfield()
