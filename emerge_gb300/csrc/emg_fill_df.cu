@@ -343,11 +343,10 @@ constexpr int kWarps = 4;
 constexpr int kKmax = kDfMaxInc;        // incidences per warp group
 constexpr int kNmax = kDfMaxCols;       // columns per entity
 constexpr int kGmax = 6;                // entities per warp group
-constexpr int kColPool = 384;           // columns of all entities of a group
+constexpr int kColPool = 256;           // columns of all entities of a group (2 edges x kNmax; 6 faces x 32)
 
 struct __align__(16) WarpSm {
     float4 stage[kKmax * 10][4];        // per item: D (4 df) then F (4 df)
-    float4 sc[kKmax][2];                // per incidence: sE, sB (re.h, re.l, im.h, im.l)
     int64_t b1[kGmax], b2[kGmax];       // CSR offsets of each entity's two rows
     int32_t cols[kColPool];             // sorted columns of each entity (pooled)
     int32_t n[kGmax], k[kGmax], cofs[kGmax], kofs[kGmax];
@@ -424,8 +423,6 @@ __global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict_
                 sm.tet[ko + q] = (int32_t)t;
                 sm.slot[ko + q] = (int8_t)(code & 15);
                 sm.qent[ko + q] = (int8_t)u;
-                sm.sc[ko + q][0] = __ldg(tscale + 2 * t);
-                sm.sc[ko + q][1] = __ldg(tscale + 2 * t + 1);
             }
             for (int q = 0; q < sm.k[u]; ++q)
                 for (int c = lane; c < n; c += 32) sm.tab[ko + q][c] = 0xff;
@@ -469,8 +466,12 @@ __global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict_
         // owner phase: position-parallel accumulation in ascending tet order
         for (int u = 0; u < nsub; ++u) {
             const int n = sm.n[u], ko = sm.kofs[u], ke = ko + sm.k[u];
+            // material scales per incidence: sE, sB (re.h, re.l, im.h, im.l), read through L1
             bool e_real = true;
-            for (int q = ko; q < ke; ++q) e_real &= (sm.sc[q][0].z == 0.f && sm.sc[q][0].w == 0.f);
+            for (int q = ko; q < ke; ++q) {
+                const float4 se = __ldg(tscale + 2 * (int64_t)sm.tet[q]);
+                e_real &= (se.z == 0.f && se.w == 0.f);
+            }
             for (int p = lane; p < n; p += 32) {
 #pragma unroll
                 for (int a = 0; a < 2; ++a) {
@@ -484,7 +485,8 @@ __global__ void __launch_bounds__(32 * kWarps) k_fill_df(const Rec2* __restrict_
                         const float4 fvv = st[2 + a];
                         const df Dv = b ? mk(dv.z, dv.w) : mk(dv.x, dv.y);
                         const df Fv = b ? mk(fvv.z, fvv.w) : mk(fvv.x, fvv.y);
-                        const float4 se = sm.sc[q][0], sb = sm.sc[q][1];
+                        const float4 se = __ldg(tscale + 2 * (int64_t)sm.tet[q]);
+                        const float4 sb = __ldg(tscale + 2 * (int64_t)sm.tet[q] + 1);
                         acc_fma(er, mk(se.x, se.y), Dv);
                         if (!e_real) acc_fma(ei, mk(se.z, se.w), Dv);
                         acc_fma(br, mk(sb.x, sb.y), Fv);
