@@ -28,27 +28,32 @@ __device__ __forceinline__ int local_of(const int32_t* tv, int32_t gid) {
     return tv[0] == gid ? 0 : tv[1] == gid ? 1 : tv[2] == gid ? 2 : 3;
 }
 
-__global__ void k_interp(int64_t np_, const double* __restrict__ pts, const double* __restrict__ nodes, int64_t nN,
-                         const int32_t* __restrict__ tets, int64_t nT, const int32_t* __restrict__ edges, int64_t nE,
-                         const int32_t* __restrict__ tris, int64_t nTri, const int32_t* __restrict__ t2f,
-                         const double2* __restrict__ sol, int64_t ntl, const int32_t* __restrict__ tetids,
-                         double2* __restrict__ E) {
-    const int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (ip >= np_) return;
-    const double px = pts[ip], py = pts[np_ + ip], pz = pts[2 * np_ + ip];
-    double2 ex = make_double2(0, 0), ey = ex, ez = ex;
+// The containing tet of point p (backwards over tetids) and its barycentric
+// numerators, their gradients and 216 V^3; false when no tet contains p.
+struct TetAt {
+    int64_t t;
+    int32_t tv[4];
+    double vx[4], vy[4], vz[4];
+    double A[4], gb[4], gc[4], gd[4];
+    double den;
+};
+
+__device__ bool locate(double px, double py, double pz, const double* __restrict__ nodes, int64_t nN,
+                       const int32_t* __restrict__ tets, int64_t nT, int64_t ntl, const int32_t* __restrict__ tetids,
+                       TetAt& r) {
     for (int64_t it = ntl - 1; it >= 0; --it) {
         const int64_t t = tetids[it];
         if (t < 0 || t >= nT) continue;
-        int32_t tv[4];
-        double vx[4], vy[4], vz[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            tv[j] = tets[j * nT + t];
-            vx[j] = nodes[tv[j]];
-            vy[j] = nodes[nN + tv[j]];
-            vz[j] = nodes[2 * nN + tv[j]];
+            r.tv[j] = tets[j * nT + t];
+            r.vx[j] = nodes[r.tv[j]];
+            r.vy[j] = nodes[nN + r.tv[j]];
+            r.vz[j] = nodes[2 * nN + r.tv[j]];
         }
+        const double* vx = r.vx;
+        const double* vy = r.vy;
+        const double* vz = r.vz;
         // local coordinates: solve [e1 e2 e3] xi = p - v1 by Cramer's rule
         const double e1x = vx[1] - vx[0], e1y = vy[1] - vy[0], e1z = vz[1] - vz[0];
         const double e2x = vx[2] - vx[0], e2y = vy[2] - vy[0], e2z = vz[2] - vz[0];
@@ -66,28 +71,51 @@ __global__ void k_interp(int64_t np_, const double* __restrict__ pts, const doub
         // permutation of ascending order), and grad det[a - p; b - p; c - p] =
         // -(b - a) x (c - a), so the coefficients (b_i, c_i, d_i) = -(-1)^i (v_k - v_j)
         // x (v_l - v_j).  det(P) = det[e1; e2; e3] = dm.
-        double A[4], gb[4], gc[4], gd[4];
-        const double detP = dm;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int j = (i + 1) & 3, k = (i + 2) & 3, l = (i + 3) & 3;
-            const double s = (i & 1) ? -1.0 : 1.0;
+            const double sg = (i & 1) ? -1.0 : 1.0;
             const double ax = vx[j] - px, ay = vy[j] - py, az = vz[j] - pz;
             const double bx = vx[k] - px, by = vy[k] - py, bz = vz[k] - pz;
             const double cx = vx[l] - px, cy = vy[l] - py, cz = vz[l] - pz;
-            A[i] = s * det3(ax, bx, cx, ay, by, cy, az, bz, cz);
-            gb[i] = -s * ((vy[k] - vy[j]) * (vz[l] - vz[j]) - (vz[k] - vz[j]) * (vy[l] - vy[j]));
-            gc[i] = -s * ((vz[k] - vz[j]) * (vx[l] - vx[j]) - (vx[k] - vx[j]) * (vz[l] - vz[j]));
-            gd[i] = -s * ((vx[k] - vx[j]) * (vy[l] - vy[j]) - (vy[k] - vy[j]) * (vx[l] - vx[j]));
+            r.A[i] = sg * det3(ax, bx, cx, ay, by, cy, az, bz, cz);
+            r.gb[i] = -sg * ((vy[k] - vy[j]) * (vz[l] - vz[j]) - (vz[k] - vz[j]) * (vy[l] - vy[j]));
+            r.gc[i] = -sg * ((vz[k] - vz[j]) * (vx[l] - vx[j]) - (vx[k] - vx[j]) * (vz[l] - vz[j]));
+            r.gd[i] = -sg * ((vx[k] - vx[j]) * (vy[l] - vy[j]) - (vy[k] - vy[j]) * (vx[l] - vx[j]));
         }
-        const double den = fabs(detP) * fabs(detP) * fabs(detP);
-        const int32_t* f = t2f + t;   // column t of (20, nT)
-        double2 rx = make_double2(0, 0), ry = rx, rz = rx;
+        r.den = fabs(dm) * fabs(dm) * fabs(dm);
+        r.t = t;
+        return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ double seg_len(const TetAt& r, int a, int b) {
+    return sqrt((r.vx[a] - r.vx[b]) * (r.vx[a] - r.vx[b]) + (r.vy[a] - r.vy[b]) * (r.vy[a] - r.vy[b]) +
+                (r.vz[a] - r.vz[b]) * (r.vz[a] - r.vz[b]));
+}
+
+__global__ void k_interp(int64_t np_, const double* __restrict__ pts, const double* __restrict__ nodes, int64_t nN,
+                         const int32_t* __restrict__ tets, int64_t nT, const int32_t* __restrict__ edges, int64_t nE,
+                         const int32_t* __restrict__ tris, int64_t nTri, const int32_t* __restrict__ t2f,
+                         const double2* __restrict__ sol, int64_t ntl, const int32_t* __restrict__ tetids,
+                         double2* __restrict__ E) {
+    const int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (ip >= np_) return;
+    const double px = pts[ip], py = pts[np_ + ip], pz = pts[2 * np_ + ip];
+    double2 rx = make_double2(0, 0), ry = rx, rz = rx;
+    TetAt r;
+    if (locate(px, py, pz, nodes, nN, tets, nT, ntl, tetids, r)) {
+        const double* A = r.A;
+        const double* gb = r.gb;
+        const double* gc = r.gc;
+        const double* gd = r.gd;
+        const double den = r.den;
+        const int32_t* f = t2f + r.t;   // column t of (20, nT)
         for (int ie = 0; ie < 6; ++ie) {
             const int32_t eid = f[ie * nT];
-            const int i1 = local_of(tv, edges[eid]), i2 = local_of(tv, edges[nE + eid]);
-            const double L = sqrt((vx[i1] - vx[i2]) * (vx[i1] - vx[i2]) + (vy[i1] - vy[i2]) * (vy[i1] - vy[i2]) +
-                                  (vz[i1] - vz[i2]) * (vz[i1] - vz[i2]));
+            const int i1 = local_of(r.tv, edges[eid]), i2 = local_of(r.tv, edges[nE + eid]);
+            const double L = seg_len(r, i1, i2);
             const double2 e1 = sol[f[ie * nT]], e2 = sol[f[(10 + ie) * nT]];
             const double2 sv = make_double2(e1.x * A[i1] + e2.x * A[i2], e1.y * A[i1] + e2.y * A[i2]);
             const double wx = L * (gb[i1] * A[i2] - gb[i2] * A[i1]) / den;
@@ -99,12 +127,10 @@ __global__ void k_interp(int64_t np_, const double* __restrict__ pts, const doub
         }
         for (int jf = 0; jf < 4; ++jf) {
             const int64_t fid = f[(6 + jf) * nT] - nE;
-            const int i1 = local_of(tv, tris[fid]), i2 = local_of(tv, tris[nTri + fid]),
-                      i3 = local_of(tv, tris[2 * nTri + fid]);
-            const double L1 = sqrt((vx[i1] - vx[i3]) * (vx[i1] - vx[i3]) + (vy[i1] - vy[i3]) * (vy[i1] - vy[i3]) +
-                                   (vz[i1] - vz[i3]) * (vz[i1] - vz[i3]));
-            const double L2 = sqrt((vx[i1] - vx[i2]) * (vx[i1] - vx[i2]) + (vy[i1] - vy[i2]) * (vy[i1] - vy[i2]) +
-                                   (vz[i1] - vz[i2]) * (vz[i1] - vz[i2]));
+            const int i1 = local_of(r.tv, tris[fid]), i2 = local_of(r.tv, tris[nTri + fid]),
+                      i3 = local_of(r.tv, tris[2 * nTri + fid]);
+            const double L1 = seg_len(r, i1, i3);
+            const double L2 = seg_len(r, i1, i2);
             const double2 e1 = sol[f[(6 + jf) * nT]], e2 = sol[f[(16 + jf) * nT]];
             const double* g[3] = {gb, gc, gd};
             double w1[3], w2[3];
@@ -117,18 +143,85 @@ __global__ void k_interp(int64_t np_, const double* __restrict__ pts, const doub
             ry.x += e1.x * w1[1] + e2.x * w2[1]; ry.y += e1.y * w1[1] + e2.y * w2[1];
             rz.x += e1.x * w1[2] + e2.x * w2[2]; rz.y += e1.y * w1[2] + e2.y * w2[2];
         }
-        ex = rx;
-        ey = ry;
-        ez = rz;
-        break;
     }
-    E[ip] = ex;
-    E[np_ + ip] = ey;
-    E[2 * np_ + ip] = ez;
+    E[ip] = rx;
+    E[np_ + ip] = ry;
+    E[2 * np_ + ip] = rz;
+}
+
+// Line functional weights: for point p with step d (e.g. a voltage-line segment),
+// the 20 DOFs of the containing tet and w_k = d . N_k(p), so that sum_k w_k x[dof_k]
+// = d . E(p) for every solution x.  No containing tet: dofs -1, weights 0.
+__global__ void k_weights(int64_t np_, const double* __restrict__ pts, const double* __restrict__ dirs,
+                          const double* __restrict__ nodes, int64_t nN, const int32_t* __restrict__ tets, int64_t nT,
+                          const int32_t* __restrict__ edges, int64_t nE, const int32_t* __restrict__ tris,
+                          int64_t nTri, const int32_t* __restrict__ t2f, int64_t ntl,
+                          const int32_t* __restrict__ tetids, int32_t* __restrict__ dof, double* __restrict__ w) {
+    const int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (ip >= np_) return;
+    const double px = pts[ip], py = pts[np_ + ip], pz = pts[2 * np_ + ip];
+    const double dx = dirs[ip], dy = dirs[np_ + ip], dz = dirs[2 * np_ + ip];
+    int32_t* od = dof + ip * 20;
+    double* ow = w + ip * 20;
+    TetAt r;
+    if (!locate(px, py, pz, nodes, nN, tets, nT, ntl, tetids, r)) {
+        for (int k = 0; k < 20; ++k) {
+            od[k] = -1;
+            ow[k] = 0.0;
+        }
+        return;
+    }
+    const double* A = r.A;
+    const double den = r.den;
+    const int32_t* f = t2f + r.t;
+    for (int ie = 0; ie < 6; ++ie) {
+        const int32_t eid = f[ie * nT];
+        const int i1 = local_of(r.tv, edges[eid]), i2 = local_of(r.tv, edges[nE + eid]);
+        const double L = seg_len(r, i1, i2);
+        // d . L (g1 A2 - g2 A1) / den, times A1 (mode 1) or A2 (mode 2)
+        const double q = L * (dx * (r.gb[i1] * A[i2] - r.gb[i2] * A[i1]) + dy * (r.gc[i1] * A[i2] - r.gc[i2] * A[i1]) +
+                              dz * (r.gd[i1] * A[i2] - r.gd[i2] * A[i1])) / den;
+        od[ie] = f[ie * nT];
+        ow[ie] = q * A[i1];
+        od[10 + ie] = f[(10 + ie) * nT];
+        ow[10 + ie] = q * A[i2];
+    }
+    for (int jf = 0; jf < 4; ++jf) {
+        const int64_t fid = f[(6 + jf) * nT] - nE;
+        const int i1 = local_of(r.tv, tris[fid]), i2 = local_of(r.tv, tris[nTri + fid]),
+                  i3 = local_of(r.tv, tris[2 * nTri + fid]);
+        const double L1 = seg_len(r, i1, i3);
+        const double L2 = seg_len(r, i1, i2);
+        const double c1 = dx * (r.gb[i1] * A[i3] - r.gb[i3] * A[i1]) + dy * (r.gc[i1] * A[i3] - r.gc[i3] * A[i1]) +
+                          dz * (r.gd[i1] * A[i3] - r.gd[i3] * A[i1]);
+        const double c2 = dx * (r.gb[i1] * A[i2] - r.gb[i2] * A[i1]) + dy * (r.gc[i1] * A[i2] - r.gc[i2] * A[i1]) +
+                          dz * (r.gd[i1] * A[i2] - r.gd[i2] * A[i1]);
+        od[6 + jf] = f[(6 + jf) * nT];
+        ow[6 + jf] = -L1 * c1 * A[i2] / den;
+        od[16 + jf] = f[(16 + jf) * nT];
+        ow[16 + jf] = L2 * c2 * A[i3] / den;
+    }
 }
 
 }  // namespace interp
 }  // namespace emg
+
+extern "C" int emg_field_weights(int64_t n_points, const double* points, const double* dirs, int64_t n_nodes,
+                                 const double* nodes, int64_t n_tets, const int32_t* tets, int64_t n_edges,
+                                 const int32_t* edges, int64_t n_tris, const int32_t* tris,
+                                 const int32_t* tet_to_field, int64_t n_tetids, const int32_t* tetids,
+                                 int32_t* dofs_out, double* weights_out, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(points && dirs && nodes && tets && edges && tris && tet_to_field && dofs_out && weights_out &&
+                      n_points >= 0 && n_tetids >= 0 && (n_tetids == 0 || tetids),
+                  "emg_field_weights: bad argument");
+    if (n_points == 0) return EMG_OK;
+    interp::k_weights<<<(unsigned)((n_points + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+        n_points, points, dirs, nodes, n_nodes, tets, n_tets, edges, n_edges, tris, n_tris, tet_to_field, n_tetids,
+        tetids, dofs_out, weights_out);
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
 
 extern "C" int emg_field_interp(int64_t n_points, const double* points, int64_t n_nodes, const double* nodes,
                                 int64_t n_tets, const int32_t* tets, int64_t n_edges, const int32_t* edges,

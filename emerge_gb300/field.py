@@ -52,3 +52,24 @@ def interpolate(field, solution, xs, ys, zs, tetids=None, device="cuda"):
               _vp(ids), _vp(E), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
     E = E.cpu().numpy()
     return E[0], E[1], E[2]
+
+
+def line_weights(field, points, dirs, tetids=None, device="cuda"):
+    """Sparse linear functional of the field: (dofs, weights), each (n_points, 20), with
+    sum(weights * x[dofs]) = sum_i dirs[:, i] . E_x(points[:, i]) for every solution x
+    (emg_field_weights).  A voltage line integral is this with the line midpoints and
+    steps (fem/physics/edm/emfreq3d.py:752-757).  Points in no tet of ``tetids`` get
+    dof -1 and weight 0.  Returns CUDA tensors (int64 dofs, float64 weights)."""
+    dev = torch.device(device)
+    nodes, tets, edges, tris, t2f = _mesh_arrays(field, dev)
+    pts = torch.as_tensor(np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(3, -1)), device=dev)
+    drs = torch.as_tensor(np.ascontiguousarray(np.asarray(dirs, dtype=np.float64).reshape(3, -1)), device=dev)
+    ids = torch.as_tensor(np.ascontiguousarray(np.arange(tets.shape[1]) if tetids is None else tetids, dtype=np.int32),
+                          device=dev)
+    n = pts.shape[1]
+    dofs = torch.empty((n, 20), dtype=torch.int32, device=dev)
+    w = torch.empty((n, 20), dtype=torch.float64, device=dev)
+    _lib.call("emg_field_weights", n, _vp(pts), _vp(drs), int(nodes.shape[1]), _vp(nodes), int(tets.shape[1]),
+              _vp(tets), int(edges.shape[1]), _vp(edges), int(tris.shape[1]), _vp(tris), _vp(t2f), int(ids.numel()),
+              _vp(ids), _vp(dofs), _vp(w), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    return dofs.to(torch.int64), w

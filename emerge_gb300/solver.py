@@ -469,6 +469,37 @@ class FrequencySweep:
         self.sys = RestrictedSystem(plan.indptr, plan.indices[: plan.nnz], plan.nnz, self.solve_ids)
         self.u_r = self.sys.gather(torch.stack([self.u[bc.port_number] for bc in self.ports]))   # (n, np)
         self.Pmode = np.array([_mode_power(field, bc) for bc in self.ports])
+        # forcing amplitude per unit port mode: U_inc = -2j beta amp E_mode (1 for waveports,
+        # whose mode carries its amplitude; V/h * 376.7303/Zs for lumped ports)
+        self.amp = np.array([_lumped_amp(bc) if _is_lumped(bc) else 1.0 for bc in self.ports])
+        self._vfun = self._voltage_functionals()
+
+    def _voltage_functionals(self):
+        """Per lumped port, its line voltage sum_i E(mid_i) . dl_i as a sparse functional of
+        the restricted solution (fem/physics/edm/emfreq3d.py:752-757), the field searched
+        over the tets that touch a port face, last containing tet winning
+        (all_port_tets, emfreq3d.py:648-653)."""
+        from .field import line_weights
+        out = {}
+        lumped = [i for i, bc in enumerate(self.ports) if _is_lumped(bc)]
+        if not lumped:
+            return out
+        m = self.field.mesh
+        verts = np.unique(np.concatenate([np.asarray(m.tris)[:, np.asarray(m.get_triangles(bc.tags), dtype=np.int64)]
+                                          .ravel() for bc in self.ports]))
+        hit = np.isin(np.asarray(m.tets), verts).any(axis=0)
+        port_tets = np.flatnonzero(hit)
+        N = self.plan.n_field
+        full2r = torch.full((N,), -1, dtype=torch.int64, device=self.device)
+        full2r[torch.as_tensor(self.solve_ids, device=self.device)] = torch.arange(self.sys.n, device=self.device)
+        for i in lumped:
+            mid, step = _lumped_line(self.ports[i], m)
+            dofs, w = line_weights(self.field, mid, step, tetids=port_tets, device=self.device)
+            dofs, w = dofs.reshape(-1), w.reshape(-1)
+            r = torch.where(dofs >= 0, full2r[dofs.clamp_min(0)], torch.full_like(dofs, -1))
+            keep = r >= 0                      # PEC DOFs hold zero
+            out[i] = (r[keep], w[keep].to(torch.complex128))
+        return out
 
     def _coeffs(self, freqs):
         k0 = 2 * np.pi * np.asarray(freqs, dtype=float) / C0
@@ -480,21 +511,39 @@ class FrequencySweep:
         """(n, nf*np) restricted right-hand sides, column f*np + p."""
         nf = beta.shape[1]
         npo = len(self.ports)
-        scale = torch.as_tensor((-2j * beta.T).reshape(-1), device=self.device)                  # (nf*np)
+        scale = torch.as_tensor((-2j * beta.T * self.amp[None, :]).reshape(-1), device=self.device)  # (nf*np)
         cols = self.u_r[:, torch.arange(npo, device=self.device).repeat(nf)]                    # (n, nf*np)
         return cols * scale[None, :]
 
-    def _sparams(self, X, nf, beta):
+    def _sparams(self, X, nf, beta, k0):
+        """S[f, i, j] = pfield_i / pmode_j for the column of frequency f driven at port j
+        (fem/physics/edm/emfreq3d.py:690-766).
+
+        Waveports (fem/mth/sparam.py:72-139): int E_c . E_mode_i = -x_c . u_i (the forcing
+        of fem/mth/tri.py:668-693 is -int N . U_inc, so u_i = -int N . E_mode_i; E_mode real),
+        pfield = (int E . E_mode - [i = j] P_i) / (2 Z_i), pmode = P_j / (2 Z_j).
+        Lumped ports (emfreq3d.py:752-766): V = line voltage, pfield = sqrt((V - [i = j] V0)^2
+        / (2 Z0)), pmode = sqrt(V0^2 / (2 Z0)), principal square roots as the reference."""
         npo = len(self.ports)
-        # int E_c . E_mode_i = -x_c . u_i: the waveport forcing of fem/mth/tri.py:668-693
-        # is -int N . U_inc (its signA * Area factor), so u_i = -int N . E_mode_i
-        # (E_mode real: no conjugation)
         G = -(self.u_r.T @ X).cpu().numpy()                                                      # (np, nf*np)
+        V = {i: (w[:, None] * X[r]).sum(dim=0).cpu().numpy() for i, (r, w) in self._vfun.items()}
         S = np.zeros((nf, npo, npo), dtype=np.complex128)
         for f in range(nf):
             for j in range(npo):
+                bj = self.ports[j]
+                if _is_lumped(bj):
+                    pm = np.sqrt(complex(bj.voltage) ** 2 / (2 * bj.Z0))
+                else:
+                    pm = self.Pmode[j] / (2 * _zmode(bj, k0[f]))
                 for i in range(npo):
-                    S[f, i, j] = (G[i, f * npo + j] - (self.Pmode[i] if i == j else 0.0)) / self.Pmode[i]
+                    bi = self.ports[i]
+                    c = f * npo + j
+                    if _is_lumped(bi):
+                        bv = V[i][c] - (bi.voltage if i == j else 0.0)
+                        pf = np.sqrt(bv ** 2 / (2 * bi.Z0))
+                    else:
+                        pf = (G[i, c] - (self.Pmode[i] if i == j else 0.0)) / (2 * _zmode(bi, k0[f]))
+                    S[f, i, j] = pf / pm
         return S
 
     def slab(self) -> SlabFactor:
@@ -611,7 +660,7 @@ class FrequencySweep:
             res[f0 * npo:f1 * npo] = rs
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
-        S = self._sparams(X, nf, beta)
+        S = self._sparams(X, nf, beta, k0)
         info = {"anchors": anchors, "precision": precision, "refine": refine, "inner": inner,
                 "refinement_steps": steps, "factor_seconds": t_fac, **sl.info()}
         return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X, info)
@@ -664,7 +713,7 @@ class FrequencySweep:
                 res[f0 * npo:f1 * npo] = rs
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
-        S = self._sparams(X, nf, beta)
+        S = self._sparams(X, nf, beta, k0)
         return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X)
 
 
@@ -719,7 +768,7 @@ class FrequencySweep:
         al = torch.as_tensor(alpha, device=self.device)                 # (nf, na)
         G = torch.einsum("fa,fb,abij->fij", al.conj(), al, Gab)          # (nf, r, r)
         h = torch.einsum("fa,api->fpi", al.conj(), Hu)                   # (nf, np, r)
-        bscale = torch.as_tensor(-2j * beta.T, device=self.device)       # (nf, np)
+        bscale = torch.as_tensor(-2j * beta.T * self.amp[None, :], device=self.device)   # (nf, np)
         h = h * bscale[:, :, None]
         # ridge-free solve; G is Hermitian positive definite on a full-rank basis
         y = torch.linalg.solve(G[:, None, :, :].expand(nf, npo, r, r), h[..., None])[..., 0]   # (nf, np, r)
@@ -840,6 +889,31 @@ class _UnitRobin:
 
     def get_Uinc(self, x, y, k0):
         return np.asarray(self.bc.port_mode_3d(x, y, k0), dtype=np.complex128)
+
+
+def _is_lumped(bc) -> bool:
+    """A port with a voltage line: this package's LumpedPort, or the reference's once
+    define_lumped_port_integration_points has set its ``vintline``."""
+    return bool(getattr(bc, "v_integration", False)) and (
+        hasattr(bc, "integration_line") or getattr(bc, "vintline", None) is not None)
+
+
+def _lumped_line(bc, mesh):
+    """(midpoints (3, n), steps (3, n)) of a lumped port's voltage line."""
+    if hasattr(bc, "integration_line"):
+        return bc.integration_line(mesh)
+    ln = bc.vintline
+    return np.array(ln.cmid), np.array([ln.dxs, ln.dys, ln.dzs])
+
+
+def _lumped_amp(bc) -> float:
+    """|U_inc| / (2 k0) of a lumped port: V/h * 376.7303 / Zs (fem/bc.py:711-713)."""
+    return float(bc.voltage) / float(bc.height) * (376.7303 / float(bc.surfZ))
+
+
+def _zmode(bc, k0) -> float:
+    z = getattr(bc, "Zmode", None)
+    return complex(z(k0)) if callable(z) else 376.730313412
 
 
 def _mode_power(field, bc) -> float:

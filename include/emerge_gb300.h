@@ -206,6 +206,18 @@ int emg_field_interp(int64_t n_points, const double* points, int64_t n_nodes, co
                      const int32_t* tet_to_field, const double* solution, int64_t n_tetids, const int32_t* tetids,
                      double* E_out, void* stream);
 
+/* Linear functionals of the field along directions: for point i with vector
+ * dirs[:, i] (3, n_points), the 20 DOFs of the containing tet (same search as
+ * emg_field_interp) in dofs_out[i*20 + k] and weights_out[i*20 + k] =
+ * dirs[:, i] . N_k(points[:, i]), so that sum_k weights * solution[dofs] =
+ * dirs . E(point) for every solution.  -1 / 0 where no tet contains the point.
+ * The voltage of a lumped port (fem/physics/edm/emfreq3d.py:752-757) is the sum
+ * of these over its line midpoints with the line steps as dirs.  DEVICE arrays. */
+int emg_field_weights(int64_t n_points, const double* points, const double* dirs, int64_t n_nodes,
+                      const double* nodes, int64_t n_tets, const int32_t* tets, int64_t n_edges, const int32_t* edges,
+                      int64_t n_tris, const int32_t* tris, const int32_t* tet_to_field, int64_t n_tetids,
+                      const int32_t* tetids, int32_t* dofs_out, double* weights_out, void* stream);
+
 /* ------------------------------------------------------- slab solver ---
  * Direct block-tridiagonal factorization of the restricted system, the
  * counterpart of the reference's direct solvers (SolverSuperLU / SolverPardiso /

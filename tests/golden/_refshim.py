@@ -103,6 +103,9 @@ class FakeGmsh(types.ModuleType):
         self.model.mesh = types.SimpleNamespace(get_nodes=self._get_nodes,
                                                 get_elements=self._get_elements)
         self.model.getEntities = lambda dim=-1: []
+        # outward normals of the boundary faces by tag (set by the fixture that needs them)
+        self.face_normals = {}
+        self.model.getNormal = lambda tag, uv: np.asarray(self.face_normals[int(tag)], dtype=float)
         self.model.get_boundary = lambda *a, **k: []
         self.model.getBoundary = self.model.get_boundary
         self.initialize = lambda *a, **k: None

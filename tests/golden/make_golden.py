@@ -25,6 +25,14 @@ Fixtures:
                      SuperLU field: 6-point quadrature points of the port-1 triangles
                      over the port tets (the S-parameter evaluation) and random
                      interior points over all tets
+  lumped.npz         parallel-plate line between two LumpedPorts (fem/bc.py:620-745) with
+                     absorbing side walls, 10 GHz: K and port-vector checksums, the
+                     voltage lines of define_lumped_port_integration_points
+                     (fem/physics/edm/emfreq3d.py:366-389), SuperLU fields and the
+                     voltage-integral S-parameters (emfreq3d.py:752-766)
+  port_elements.npz  generalized_matrix_GQ (fem/physics/edm/nedeleclegrange2.py:224-382), the
+                     14x14 element matrices of the 2-D port mode problem, on 24 triangles with
+                     random edge orientations and isotropic / anisotropic materials
   farfield.npz       stratton_chu (fem/physics/edm/sc.py:143-180) of a short dipole's
                      near field sampled at the edge centres of a closed box surface
 """
@@ -339,6 +347,110 @@ def make_interp():
                         port_E=np.stack(Ep), inner_points=inner, inner_E=np.stack(Ei), inner_tets=tsel)
 
 
+def lumped_mesh(h=1e-3):
+    L, W, H = 0.015, 0.006, 0.002
+    nx, ny, nz = int(round(L / h)), int(round(W / h)), int(round(H / h))
+    return structured_box(np.linspace(0, L, nx + 1), np.linspace(0, W, ny + 1), np.linspace(0, H, nz + 1)), (L, W, H)
+
+
+def make_lumped():
+    """Two lumped ports (x = 0 and x = L faces, E along +z) on a parallel-plate line:
+    PEC plates at z = 0 and z = H, first-order absorbing walls at y = 0 and y = W."""
+    tm, (L, W, H) = lumped_mesh()
+    m = reference_mesh(tm)
+    GMSH.face_normals = {pm.FACE_XMIN: (-1.0, 0, 0), pm.FACE_XMAX: (1.0, 0, 0)}
+    field = Nedelec2(m)
+    nT = m.n_tets
+    er = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2) * (2.2 - 0.01j)
+    ur = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    from fem.cs import ZAX
+    p1 = ref_bc.LumpedPort(FaceSelection([pm.FACE_XMIN]), 1, width=W, height=H, direction=ZAX, Z0=50.0)
+    p2 = ref_bc.LumpedPort(FaceSelection([pm.FACE_XMAX]), 2, width=W, height=H, direction=ZAX, Z0=50.0)
+    abc = ref_bc.AbsorbingBoundary(FaceSelection([pm.FACE_YMIN, pm.FACE_YMAX]))
+    pec = ref_bc.PEC(FaceSelection([pm.FACE_ZMIN, pm.FACE_ZMAX]))
+    bcs = [pec, abc, p1, p2]
+    phys = Electrodynamics3D.__new__(Electrodynamics3D)
+    phys.mesh = m
+    for p in (p1, p2):
+        phys.define_lumped_port_integration_points(p)
+    asm = ref_assembler.Assembler()
+    routine = ref_solver.SolveRoutine(ref_solver.ReverseCuthillMckee(), ref_solver.Preconditioner(), None,
+                                      ref_solver.SolverSuperLU(), None, None)
+    routine.use_preconditioner = False
+    f = 10e9
+    k0 = 2 * np.pi * f / C0
+    K, bvec, solve_ids, pvecs = asm.assemble_freq_matrix(field, er, ur, bcs, f, cache_matrices=True)
+    out = mesh_arrays(m)
+    out["tet_to_field"] = field.tet_to_field.astype(np.int32)
+    out["tri_to_field"] = field.tri_to_field.astype(np.int32)
+    out["dims"] = np.array([L, W, H])
+    out["freq"] = f
+    out["er"] = np.complex128(2.2 - 0.01j)
+    Kc = K.tocsr()
+    out["K_rowsum"] = np.asarray(Kc.sum(axis=1)).ravel()
+    out["K_rowmom"] = Kc @ ((np.arange(Kc.shape[0]) + 1.0) / Kc.shape[0])
+    out["solve_ids"] = solve_ids.astype(np.int32)
+    verts = set()
+    for p in (p1, p2):
+        tris = m.get_triangles(p.tags)
+        p._tri_ids = tris
+        p._tri_vertices = m.tris[:, tris]
+        verts.update(set(p._tri_vertices.ravel().tolist()))
+        out[f"port_tris_{p.port_number}"] = tris.astype(np.int32)
+        nz = np.nonzero(pvecs[p.port_number])[0]
+        out[f"pvec_{p.port_number}_idx"] = nz.astype(np.int32)
+        out[f"pvec_{p.port_number}_val"] = pvecs[p.port_number][nz]
+        ln = p.vintline
+        out[f"line_{p.port_number}_mid"] = np.array(ln.cmid)
+        out[f"line_{p.port_number}_d"] = np.array([ln.dxs, ln.dys, ln.dzs])
+        out[f"gamma_{p.port_number}"] = np.complex128(p.get_gamma(k0))
+    out["pec_tris"] = m.get_triangles(pec.tags).astype(np.int32)
+    out["abc_tris"] = m.get_triangles(abc.tags).astype(np.int32)
+    port_tets = np.array([t for t in range(nT) if not set(m.tets[:, t].tolist()).isdisjoint(verts)])
+    out["port_tets"] = port_tets.astype(np.int32)
+    S = np.zeros((2, 2), dtype=np.complex128)
+    eye = lambda p: np.repeat(np.eye(3)[:, :, None], len(p._tri_ids), 2)  # noqa: E731
+    for active in (p1, p2):
+        active.active = True
+        sol = routine.solve(K, bvec + pvecs[active.port_number], solve_ids, reuse=False)
+        out[f"x_{active.port_number}"] = sol
+        fieldf = field.interpolate_Ef(sol, tetids=port_tets)
+        _, pmode = phys._compute_s_data(active, fieldf, active._tri_vertices, k0, eye(active), eye(active))
+        for bcp in (p1, p2):
+            pf, _ = phys._compute_s_data(bcp, fieldf, bcp._tri_vertices, k0, eye(bcp), eye(bcp))
+            S[bcp.port_number - 1, active.port_number - 1] = pf / pmode
+        active.active = False
+    out["S"] = S
+    print(f"lumped: {nT} tets, |S11|={abs(S[0, 0]):.4f} |S21|={abs(S[1, 0]):.4f}")
+    np.savez_compressed(os.path.join(HERE, "lumped.npz"), **out)
+
+
+def make_port_elements():
+    from fem.physics.edm import nedeleclegrange2 as ref_nl
+    rng = np.random.default_rng(77)
+    n = 24
+    verts = np.zeros((n, 2, 3))
+    lem = np.zeros((n, 2, 3), dtype=np.int64)
+    Ms = np.zeros((n, 3, 3), dtype=np.complex128)
+    Mm = np.zeros((n, 3, 3), dtype=np.complex128)
+    k0 = rng.uniform(100, 400, n)
+    A = np.zeros((n, 14, 14), dtype=np.complex128)
+    B = np.zeros((n, 14, 14), dtype=np.complex128)
+    pairs = [(0, 1), (1, 2), (0, 2)]
+    for k in range(n):
+        h = 10 ** rng.uniform(-3.5, -2)
+        v = rng.uniform(-1, 1, (2, 3)) * h + rng.uniform(-0.05, 0.05, (2, 1))
+        verts[k] = v
+        for e, (a, b) in enumerate(pairs):
+            lem[k, :, e] = (a, b) if rng.random() < 0.5 else (b, a)
+        Ms[k] = _rand_c3(rng, k % 3 == 0)
+        Mm[k] = _rand_c3(rng, k % 3 == 0)
+        A[k], B[k] = ref_nl.generalized_matrix_GQ(v, lem[k], Ms[k], Mm[k], float(k0[k]))
+    np.savez_compressed(os.path.join(HERE, "port_elements.npz"), verts=verts, local_edge_map=lem, Ms=Ms, Mm=Mm,
+                        k0=k0, A=A, B=B)
+    print(f"port_elements: {n} triangles")
+
+
 def dipole_surface(h=6e-3, half=0.03, k0=2 * np.pi * 10e9 / C0, seed=5):
     """A closed box surface around a z-directed short dipole at the origin.
 
@@ -407,7 +519,7 @@ def make_farfield():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc", "interp", "farfield"]
+    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc", "interp", "lumped", "port", "farfield"]
     if "tet" in which:
         make_tet_elements()
     if "tri" in which:
@@ -420,5 +532,9 @@ if __name__ == "__main__":
         make_waveguide_abc()
     if "interp" in which:
         make_interp()
+    if "lumped" in which:
+        make_lumped()
+    if "port" in which:
+        make_port_elements()
     if "farfield" in which:
         make_farfield()
