@@ -36,6 +36,8 @@ SIGNATURES = {
     "emg_edge_lengths": (ctypes.c_int, [c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "emg_field_weights": (ctypes.c_int, [c_i64, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp,
                                          c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "emg_port_element_matrices": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_int, c_vp,
+                                                 c_vp, c_vp]),
     "emg_stratton_chu": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, ctypes.c_float, c_vp,
                                         c_vp, c_vp]),
     "emg_assemble_tet_tensor_host": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

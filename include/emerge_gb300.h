@@ -367,6 +367,21 @@ void emg_topology_destroy(emg_topology* topo);
 int emg_edge_lengths(int64_t n_nodes, const double* nodes, int64_t n_edges, const int32_t* edges, double* lengths,
                      void* stream);
 
+/* ---------------------------------------------------------- port modes ---
+ * Element matrices of the 2-D waveguide-port eigenproblem A x = lambda B x
+ * (lambda = -beta^2), the counterpart of generalized_matrix_GQ
+ * (fem/physics/edm/nedeleclegrange2.py:224-382): second-order Nedelec transverse
+ * and Lagrange longitudinal functions, 14 DOFs per triangle.  xy (2, 3, n_tris):
+ * local port-plane coordinates of each triangle's vertices; local_edge_map
+ * (2, 3, n_tris) int32: local vertex indices of each triangle edge; Ms9 =
+ * matinv(ur), Mm9 = er, complex (9, n_tris) as for emg_assemble_tet_tensor.
+ * face_block = 0 keeps the reference's zero face-face entries of the transverse
+ * B block; 1 integrates them (the consistent discretisation).
+ * A_out, B_out: (n_tris, 14, 14) complex.  DEVICE arrays; one block per triangle. */
+int emg_port_element_matrices(int64_t n_tris, const double* xy, const int32_t* local_edge_map, const double* Ms9,
+                              const double* Mm9, double k0, int face_block, double* A_out, double* B_out,
+                              void* stream);
+
 /* --------------------------------------------------------- far field ---
  * Stratton-Chu transform, the counterpart of stratton_chu_ff
  * (fem/physics/edm/sc.py:26-140).  Sources j < n_src at vis (3, n_src) f32 with

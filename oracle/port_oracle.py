@@ -36,8 +36,9 @@ DPTS = np.array([[0.22338159, 0.22338159, 0.22338159, 0.10995174, 0.10995174, 0.
                  [0.44594849, 0.10810302, 0.44594849, 0.09157621, 0.81684757, 0.09157621]])
 
 
-def element_matrices(verts, lem, Ms, Mm, k0):
-    """(A, B) 14x14 complex of one triangle: verts (2, 3), lem (2, 3) local edge map."""
+def element_matrices(verts, lem, Ms, Mm, k0, face_block=False):
+    """(A, B) 14x14 complex of one triangle: verts (2, 3), lem (2, 3) local edge map.
+    face_block: integrate the face-face entries of Dtt instead of the reference's zeros."""
     x, y = np.asarray(verts, dtype=float)[0], np.asarray(verts, dtype=float)[1]
     W = DPTS[0]
     xs = x[0] * DPTS[1] + x[1] * DPTS[2] + x[2] * DPTS[3]
@@ -98,6 +99,8 @@ def element_matrices(verts, lem, Ms, Mm, k0):
         for j in (3, 7):
             Att[i, j] = np.sum(W * C[i] * Msz * C[j])
             Btt[i, j] = dot(N[i], Mmt, N[j])
+            if face_block:
+                Dtt[i, j] = dot(N[i], Mst, N[j])
     for k in range(6):
         for j in range(8):
             Dzt[k, j] = dot(Gz[k], Mst, N[j])
