@@ -273,6 +273,7 @@ def run_gpu(args, rank, world):
     }
     if rank == 0:
         out["topology"] = run_topology(m, n, dev)
+        out["farfield"] = run_farfield(dev)
     if rank == 0 and not args.no_sweep:
         del E, B, pin_E, pin_B, npE, npB, plan
         torch.cuda.empty_cache()
@@ -421,6 +422,73 @@ def run_sweep(args):
                                    "converged": bool(ilu.residuals.max() <= args.sweep_tol * 10)}
     if args.sweep_cpu > 0:
         out["cpu_superlu"] = cpu_superlu(sw, freqs[idx[:args.sweep_cpu]], plain)
+    return out
+
+
+# FP32 operations of one (source, direction) term of k_ff_sum (multiply and add counted
+# separately, sincosf excluded): phase 5, r x (n x H) 18, n x E - Z0 (...) 12,
+# rotation by G 18, accumulation of r x ie 24
+FF_FLOPS_PER_PAIR = 77
+FP32_TFLOPS = 74.8         # GB300 FP32 FMA throughput measured by a probe kernel
+
+
+def run_farfield(dev):
+    """Stratton-Chu far field: 20k surface sources x 181 x 360 directions on the GPU,
+    against the NumPy restatement on a 300-direction sample of the same sources."""
+    import types
+    import torch
+    from emerge_gb300.farfield import stratton_chu
+    rng = np.random.default_rng(3)
+    ns, nt = 20000, 30000
+    mesh = types.SimpleNamespace(n_tris=nt, tri_to_edge=rng.integers(0, ns, (3, nt)),
+                                 normals=rng.normal(size=(3, nt)), areas=rng.uniform(1e-6, 2e-6, nt),
+                                 edge_centers=rng.uniform(-0.1, 0.1, (3, ns)))
+    E = rng.normal(size=(3, ns)) + 1j * rng.normal(size=(3, ns))
+    H = (rng.normal(size=(3, ns)) + 1j * rng.normal(size=(3, ns))) / 377
+    th, ph = np.meshgrid(np.linspace(-np.pi / 2, np.pi / 2, 181), np.linspace(0, 2 * np.pi, 360, endpoint=False),
+                         indexing="ij")
+    th, ph = th.ravel(), ph.ravel()
+    k0 = 2 * np.pi * 10e9 / 299792458
+    import ctypes
+    from emerge_gb300 import _lib
+    from emerge_gb300.farfield import surface_weights
+    t0 = time.perf_counter()
+    Eg, _ = stratton_chu(E, H, mesh, th, ph, k0, dev)                       # also the warm-up
+    t_call = time.perf_counter() - t0
+    # the device entry point alone, inputs resident: the transform's own time
+    d = {k: torch.as_tensor(np.ascontiguousarray(v), device=dev) for k, v in
+         (("E", E.astype(np.complex64)), ("H", H.astype(np.complex64)),
+          ("v", mesh.edge_centers.astype(np.float32)), ("w", surface_weights(mesh)),
+          ("th", th.astype(np.float32)), ("ph", ph.astype(np.float32)))}
+    Eo_d = torch.empty((3, th.size), dtype=torch.complex128, device=dev)
+    Ho_d = torch.empty_like(Eo_d)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())                                          # noqa: E731
+    reps = 5
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        _lib.call("emg_stratton_chu", ns, vp(d["E"]), vp(d["H"]), vp(d["v"]), vp(d["w"]), th.size, vp(d["th"]),
+                  vp(d["ph"]), ctypes.c_float(k0), vp(Eo_d), vp(Ho_d),
+                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    t_gpu = (time.perf_counter() - t0) / reps
+    pairs = ns * th.size
+    out = {"workload": f"{ns} sources x {th.size} directions (181 x 360), 10 GHz",
+           "device_call_s": round(t_gpu, 5), "host_call_s": round(t_call, 4), "pairs_per_s": pairs / t_gpu,
+           "compute": {"bound": "fp32", "flops_per_pair": FF_FLOPS_PER_PAIR, "peak_tflops": FP32_TFLOPS,
+                       "achieved_tflops": pairs * FF_FLOPS_PER_PAIR / t_gpu / 1e12,
+                       "frac": pairs * FF_FLOPS_PER_PAIR / t_gpu / 1e12 / FP32_TFLOPS,
+                       "note": "emg_stratton_chu wall time with device-resident inputs (its scratch "
+                               "allocation and final synchronisation included); sincosf not counted"}}
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from oracle import farfield_oracle as fo
+    wns = surface_weights(mesh)
+    sel = np.arange(0, th.size, th.size // 300)[:300]
+    t0 = time.perf_counter()
+    Eo, _ = fo.stratton_chu_ff(E, H, mesh.edge_centers, wns, th[sel], ph[sel], k0)
+    t_cpu = time.perf_counter() - t0
+    out["cpu_baseline"] = {"pairs_per_s": ns * sel.size / t_cpu, "kind": "port", "cores": os.cpu_count(),
+                           "sample": f"{sel.size} of the directions, NumPy FP64 restatement"}
+    out["max_rel_diff_vs_port"] = float(np.abs(Eg[:, sel] - Eo).max() / np.abs(Eo).max())
     return out
 
 
