@@ -568,7 +568,7 @@ def cpu_superlu(sw, freqs, plain):
         Xs = lu.solve(rhs[perm, f * npo:(f + 1) * npo])
         X = np.empty_like(Xs)
         X[perm] = Xs
-        S = sw._sparams(torch.as_tensor(X, device=sw.device), 1, beta[:, f:f + 1])
+        S = sw._sparams(torch.as_tensor(X, device=sw.device), 1, beta[:, f:f + 1], k0[f:f + 1])
         err = max(err, float(np.max(np.abs(S[0] - plain.S[f]))))
     secs = time.perf_counter() - t0
     return {"value": len(freqs) / secs, "unit": "freq-pts/s", "points": len(freqs), "cores": os.cpu_count(),
