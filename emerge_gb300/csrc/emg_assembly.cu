@@ -828,28 +828,54 @@ extern "C" int emg_assemble_tet(emg_plan* p, const double* eps, const double* mu
     return EMG_OK;
 }
 
+namespace {
+// Device address of ``n`` bytes of page-locked host memory at ``h`` (cudaHostAlloc'd or
+// registered, mapped into the device's address space), or nullptr when either end of
+// the range is not page-locked host memory.
+void* mapped_host_range(void* h, size_t n) {
+    cudaPointerAttributes a0, a1;
+    if (cudaPointerGetAttributes(&a0, h) != cudaSuccess ||
+        cudaPointerGetAttributes(&a1, static_cast<char*>(h) + (n - 1)) != cudaSuccess) {
+        cudaGetLastError();   // an unknown pointer: clear the error for later calls
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+        return nullptr;
+    if (static_cast<char*>(a1.devicePointer) - static_cast<char*>(a0.devicePointer) != (ptrdiff_t)(n - 1))
+        return nullptr;
+    return a0.devicePointer;
+}
+}  // namespace
+
 extern "C" int emg_assemble_tet_host(emg_plan* p, const double* eps, const double* mu_inv, double* E_data,
                                      double* B_data, void* stream) {
     using namespace emg;
     EMG_CHECK_ARG(p != nullptr, "emg_assemble_tet_host: NULL plan");
     EMG_CHECK_ARG(p->nnz == 0 || (eps && mu_inv && E_data && B_data), "emg_assemble_tet_host: NULL array");
     cudaStream_t s = (cudaStream_t)stream;
+    // Page-locked outputs: the fill stores its write-once values straight into them
+    // over the host link, so the element arithmetic overlaps the transfer (the link,
+    // not HBM, bounds this call).  Pageable outputs: fill into device staging, then copy.
+    const size_t vbytes = sizeof(double) * 2 * (size_t)p->nnz;
+    double* Ed = p->nnz > 0 ? static_cast<double*>(mapped_host_range(E_data, vbytes)) : nullptr;
+    double* Bd = p->nnz > 0 ? static_cast<double*>(mapped_host_range(B_data, vbytes)) : nullptr;
+    const bool direct = Ed && Bd;
     {
         int rc;
         if (!p->eps_dev && (rc = dalloc(&p->eps_dev, 2 * p->nT, "eps staging"))) return rc;
         if (!p->mu_dev && (rc = dalloc(&p->mu_dev, 2 * p->nT, "mu staging"))) return rc;
-        if (!p->E_dev && (rc = dalloc(&p->E_dev, 2 * p->nnz, "E staging"))) return rc;
-        if (!p->B_dev && (rc = dalloc(&p->B_dev, 2 * p->nnz, "B staging"))) return rc;
+        if (!direct && !p->E_dev && (rc = dalloc(&p->E_dev, 2 * p->nnz, "E staging"))) return rc;
+        if (!direct && !p->B_dev && (rc = dalloc(&p->B_dev, 2 * p->nnz, "B staging"))) return rc;
     }
     if (p->nT > 0) {
         EMG_CUDA(cudaMemcpyAsync(p->eps_dev, eps, sizeof(double) * 2 * p->nT, cudaMemcpyHostToDevice, s));
         EMG_CUDA(cudaMemcpyAsync(p->mu_dev, mu_inv, sizeof(double) * 2 * p->nT, cudaMemcpyHostToDevice, s));
     }
-    int rc = emg_assemble_tet(p, p->eps_dev, p->mu_dev, p->E_dev, p->B_dev, stream);
+    int rc = emg_assemble_tet(p, p->eps_dev, p->mu_dev, direct ? Ed : p->E_dev, direct ? Bd : p->B_dev, stream);
     if (rc) return rc;
-    if (p->nnz > 0) {
-        EMG_CUDA(cudaMemcpyAsync(E_data, p->E_dev, sizeof(double) * 2 * p->nnz, cudaMemcpyDeviceToHost, s));
-        EMG_CUDA(cudaMemcpyAsync(B_data, p->B_dev, sizeof(double) * 2 * p->nnz, cudaMemcpyDeviceToHost, s));
+    if (!direct && p->nnz > 0) {
+        EMG_CUDA(cudaMemcpyAsync(E_data, p->E_dev, vbytes, cudaMemcpyDeviceToHost, s));
+        EMG_CUDA(cudaMemcpyAsync(B_data, p->B_dev, vbytes, cudaMemcpyDeviceToHost, s));
     }
     EMG_CUDA(cudaStreamSynchronize(s));
     return EMG_OK;

@@ -73,7 +73,10 @@ int emg_assemble_tet(emg_plan* plan, const double* eps, const double* mu_inv, do
 /* Same as emg_assemble_tet with HOST arrays (eps, mu_inv: n_tets complex;
  * E_data, B_data: nnz complex): copies the materials in and the values out
  * around the device call and synchronises ``stream``.  This is the call a
- * host-side binding of tet_mass_stiffness_matrices makes. */
+ * host-side binding of tet_mass_stiffness_matrices makes.  When E_data and
+ * B_data are page-locked (cudaHostAlloc'd or cudaHostRegister'ed), the fill
+ * stores the values straight into them, overlapping the element arithmetic with
+ * the device-to-host transfer; pageable outputs go through device staging. */
 int emg_assemble_tet_host(emg_plan* plan, const double* eps, const double* mu_inv, double* E_data,
                           double* B_data, void* stream);
 

@@ -92,6 +92,12 @@ def test_device_path_is_deterministic(torch_cuda):
     Eh, Bh = plan.assemble_host(eps, mu_inv)
     assert np.array_equal(Eh.view(np.float64), torch.view_as_real(E1).cpu().numpy().ravel())
     assert np.array_equal(Bh.view(np.float64), torch.view_as_real(B1).cpu().numpy().ravel())
+    # page-locked outputs (the fill stores into host memory directly): same bits
+    pE = torch.zeros(plan.nnz, dtype=torch.complex128, pin_memory=True)
+    pB = torch.zeros(plan.nnz, dtype=torch.complex128, pin_memory=True)
+    plan.assemble_host(eps, mu_inv, pE.numpy(), pB.numpy())
+    assert np.array_equal(pE.numpy().view(np.float64), torch.view_as_real(E1).cpu().numpy().ravel())
+    assert np.array_equal(pB.numpy().view(np.float64), torch.view_as_real(B1).cpu().numpy().ravel())
 
 
 def test_empty_mesh_and_boundary_only_entities(torch_cuda):
