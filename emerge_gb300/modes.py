@@ -15,8 +15,10 @@ and ``Assembler.assemble_bma_matrices`` (fem/physics/edm/assembler.py:244-303):
 4. PEC: every DOF of a face edge that lies on a PEC triangle (its two transverse
    DOFs, its z DOF and its two vertex DOFs, assembler.py:268-293) is removed.
 5. A x = lambda B x on the remaining DOFs, dense: the reference calls LAPACK's
-   generalized eig (fem/solver.py:316-341); here B^-1 A is formed by a GPU LU solve
-   and its eigenvalues by the library's dense eigensolver on the device.
+   generalized eig (fem/solver.py:316-341).  Here the shifted inverse
+   (A - s B)^-1 B, s = -t^2, is formed by a GPU LU solve and its eigenvalues mu by
+   the library's dense eigensolver on the device; lambda = s + 1/mu.  Like QZ this
+   tolerates a singular B (its infinite eigenvalues become mu = 0).
 6. Modes with -8 t^2 <= lambda <= -1 are kept and ordered by |sqrt(-lambda) - t|,
    t = the target propagation constant (filter_real_modes, fem/solver.py:34-68).
 
@@ -163,12 +165,16 @@ def port_modes(field, er, ur, port_tags, basis, k0: float, pec_tags=(), target_k
     sid = torch.as_tensor(solve_ids, device=dev)
     As = A[sid][:, sid]
     Bs = B[sid][:, sid]
-    lam, vec = torch.linalg.eig(torch.linalg.solve(Bs, As))
-    lam = lam.cpu().numpy()
     if target_kz is None:
         d = np.concatenate([er_t[0, 0], er_t[1, 1], er_t[2, 2]])
         u = np.concatenate([ur_t[0, 0], ur_t[1, 1], ur_t[2, 2]])
         target_kz = float(np.mean(d.real) * np.mean(u.real) * 0.65 * k0)
+    sigma = -float(target_kz) ** 2
+    mu, vec = torch.linalg.eig(torch.linalg.solve(As - sigma * Bs, Bs))
+    mu = mu.cpu().numpy()
+    finite = np.abs(mu) > 1e-12 * np.abs(mu).max()
+    lam = np.full(mu.shape, np.inf + 0j)
+    lam[finite] = sigma + 1.0 / mu[finite]
     lr = lam.real
     keep = np.flatnonzero((lr <= -1) & (lr >= -(target_kz ** 2) * 8))
     beta = np.sqrt(-lam[keep])
