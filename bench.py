@@ -180,6 +180,7 @@ def run_gpu(args, rank, world):
     import torch
     from emerge_gb300 import _build
     from emerge_gb300.assembly import AssemblyPlan, material_scalars
+    from emerge_gb300.replicas import max_over_ranks
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     _build.build()
@@ -221,11 +222,9 @@ def run_gpu(args, rank, world):
         time.sleep(0.3)
     total_ms = t_begin.elapsed_time(t_end)
     launch_ms = [s.elapsed_time(x) for s, x in zip(starts, ends)]
-    ms = total_ms / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    # replicas: every rank assembles its own copy of the workload (weak scaling); the
+    # job's time is the slowest rank's
+    ms = max_over_ranks(total_ms / args.steps, device=dev)
     value = world * m.n_tets / (ms / 1e3)
 
     # end to end through the host entry point: materials H2D + E/B D2H inside the timed region
@@ -242,7 +241,7 @@ def run_gpu(args, rank, world):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         plan.assemble_host(npe, npm, npE, npB)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, device=dev)
     e2e_val = world * m.n_tets / e2e_s
 
     nnz, nT, nN = plan.nnz, m.n_tets, m.n_nodes
