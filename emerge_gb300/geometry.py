@@ -9,6 +9,9 @@ and their surfaces made PEC.  All lengths in metres.
 * ``iris_filter`` — five-cavity WR-90 bandpass filter: six inductive irises
   2 mm thick with centred apertures [12.0, 8.5, 7.8, 7.8, 8.5, 12.0] mm, cavity
   lengths [15.8, 17.6, 18.0, 17.6, 15.8] mm, 10 mm feed guides.
+* ``patch_antenna`` — rectangular patch on a lossy substrate over a finite ground
+  plane, fed by a lumped port between ground and patch, in an air box closed by
+  first-order absorbing walls (the patch benchmark's layout at a coarser grid).
 * ``dielectric_cavity`` — PEC box with a centred full-height dielectric cylinder
   (staircased on the grid), the eigenmode workload; ``cavity_set`` draws a batch
   of them from a seed.
@@ -19,7 +22,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .bc import PEC, CoordinateSystem, RectangularWaveguide
+from .bc import PEC, AbsorbingBoundary, CoordinateSystem, LumpedPort, RectangularWaveguide
 from .mesh import FACE_XMAX, FACE_XMIN, FACE_YMAX, FACE_YMIN, FACE_ZMAX, FACE_ZMIN, Nedelec2Basis, TetMesh, structured_box
 
 TAG_PORT1, TAG_PORT2, TAG_PEC = 11, 12, 13
@@ -107,6 +110,66 @@ def iris_filter(h: float = 2e-3, a: float = 0.02286, b: float = 0.01016, t: floa
         return m.astype(np.int64)
 
     return _guide_problem(xs, ys, zs, metal, a, b, L, f"5-cavity WR-90 iris filter, h={h * 1e3:.2f} mm")
+
+
+TAG_GROUND, TAG_PATCH, TAG_FEED = 21, 22, 23
+
+
+def _plane_tris(mesh: TetMesh, axis: int, value: float, lo, hi) -> np.ndarray:
+    """(3, n) vertex triples of the mesh faces in the plane x_axis = value whose other two
+    coordinates lie in [lo, hi] (per axis, ascending axis order)."""
+    P = mesh.nodes[:, mesh.tris]                                   # (3, 3, nTri)
+    tol = 1e-9
+    on = np.all(np.abs(P[axis] - value) < tol, axis=0)
+    for k, a in enumerate([a for a in range(3) if a != axis]):
+        on &= np.all((P[a] >= lo[k] - tol) & (P[a] <= hi[k] + tol), axis=0)
+    return mesh.tris[:, on]
+
+
+def patch_antenna(h_air: float = 12.5e-3, h_patch: float = 5e-3, L: float = 40e-3, W: float = 30e-3,
+                  t: float = 1.52e-3, ground: float = 80e-3, margin: float = 37.5e-3, eps_r: float = 3.38,
+                  tand: float = 0.0027, feed_x: float = -10e-3, feed_w: float = 5e-3, Z0: float = 50.0) -> Problem:
+    """Patch antenna: an L x W PEC patch at z = t on a t-thick substrate (eps_r (1 - j tand)),
+    over a ground x ground PEC plane at z = 0, in an air box ``margin`` beyond the ground
+    on every side (below included) with first-order absorbing walls.  A lumped port
+    (``Z0``, E along +z) fills the ``feed_w`` x t rectangle at x = feed_x, centred in y,
+    between ground and patch.  The grid is snapped to every edge; spacing at most
+    h_patch over the ground plane, h_air outside, one cell across the substrate."""
+    g, B = ground / 2, ground / 2 + margin
+    xb = sorted({-B, -g, -L / 2, feed_x, L / 2, g, B})
+    yb = sorted({-B, -g, -W / 2, -feed_w / 2, feed_w / 2, W / 2, g, B})
+
+    def lines(breaks):
+        out = [breaks[0]]
+        for a, b in zip(breaks[:-1], breaks[1:]):
+            h = h_patch if (a >= -g - 1e-12 and b <= g + 1e-12) else h_air
+            n = max(1, int(np.ceil((b - a) / h - 1e-9)))
+            out.extend(list(a + (b - a) * np.arange(1, n + 1) / n))
+        return np.array(out)
+
+    xs, ys = lines(xb), lines(yb)
+    zs = np.concatenate([_lines([-margin, 0.0], h_air), [t], _lines([t, t + margin], h_air)[1:]])
+
+    def substrate(cx, cy, cz):
+        return ((np.abs(cx) < g) & (np.abs(cy) < g) & (cz > 0) & (cz < t)).astype(np.int64)
+
+    box = structured_box(xs, ys, zs, cell_tag_fn=substrate)
+    bnd = dict(box.boundary)
+    bnd[TAG_GROUND] = _plane_tris(box, 2, 0.0, (-g, -g), (g, g))
+    bnd[TAG_PATCH] = _plane_tris(box, 2, t, (-L / 2, -W / 2), (L / 2, W / 2))
+    bnd[TAG_FEED] = _plane_tris(box, 0, feed_x, (-feed_w / 2, 0.0), (feed_w / 2, t))
+    mesh = TetMesh(box.nodes, box.tets, boundary=bnd, cell_tag=box.cell_tag)
+    field = Nedelec2Basis(mesh)
+    nT = mesh.n_tets
+    er = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    er[[0, 1, 2], [0, 1, 2], :] = np.where(mesh.cell_tag == 1, eps_r * (1 - 1j * tand), 1.0)[None, :]
+    ur = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    feed = LumpedPort([TAG_FEED], 1, width=feed_w, height=t, direction=(0, 0, 1), normal=(1, 0, 0), Z0=Z0)
+    bcs = [PEC([TAG_GROUND, TAG_PATCH]),
+           AbsorbingBoundary([FACE_XMIN, FACE_XMAX, FACE_YMIN, FACE_YMAX, FACE_ZMIN, FACE_ZMAX]), feed]
+    return Problem(mesh, field, bcs, er, ur,
+                   f"patch {L * 1e3:.0f}x{W * 1e3:.0f} mm on {t * 1e3:.2f} mm eps_r={eps_r}, ground "
+                   f"{ground * 1e3:.0f} mm, air margin {margin * 1e3:.1f} mm, h={h_patch * 1e3:.1f}/{h_air * 1e3:.1f} mm")
 
 
 def dielectric_cavity(a: float, b: float, c: float, radius: float, eps_r: float, h: float) -> Problem:

@@ -546,16 +546,24 @@ class FrequencySweep:
                     S[f, i, j] = pf / pm
         return S
 
-    def slab(self) -> SlabFactor:
-        """The slab structure of the restricted system (built on first use).  Slabs are
-        cross-sections of the guide: the search starts from the DOFs on the first
-        port's face."""
+    def slab(self, seeds: str = "port") -> SlabFactor:
+        """The slab structure of the restricted system (built on first use).
+
+        ``seeds="port"``: the search starts from the DOFs on the first port's face, so
+        the slabs are cross-sections of a guide.  ``seeds="axis"``: it starts from the
+        DOFs of least coordinate along the domain's longest axis, so the slabs are
+        planar cross-sections of the whole domain, which suits open structures fed by a
+        small port (the port seeds would grow shells around it)."""
         if getattr(self, "_slab", None) is None:
-            seeds = None
-            if self.ports:
+            sd = None
+            if seeds == "axis":
+                ext = np.ptp(np.asarray(self.field.mesh.nodes), axis=1)
+                sd = face_seeds(self.field, self.solve_ids, int(np.argmax(ext)))
+            elif self.ports:
                 u = self.u[self.ports[0].port_number].abs().cpu().numpy()
                 on_port = np.flatnonzero(u[self.solve_ids] > 0)
-                seeds = on_port if on_port.size else None
+                sd = on_port if on_port.size else None
+            seeds = sd
             self._slab = SlabFactor(self.sys, seeds, locality_key(self.field, self.solve_ids))
             self._slab_key = None
         return self._slab
