@@ -109,3 +109,37 @@ def test_locality_key_pairs_entity_dofs():
     for g, i in pos.items():
         if g < nE + nF and g + nE + nF in pos:
             assert key[pos[g + nE + nF]] == key[i] + 1
+
+
+def test_patch_antenna_geometry():
+    """Interior PEC sheets, the feed sheet and the substrate of the patch case."""
+    from emerge_gb300.geometry import TAG_FEED, TAG_GROUND, TAG_PATCH, patch_antenna
+    p = patch_antenna()
+    m = p.mesh
+    z = m.nodes[2]
+    g = m.nodes[:, m.boundary[TAG_GROUND]]
+    assert np.all(np.abs(g[2]) < 1e-12) and np.all(np.abs(g[:2]) <= 0.04 + 1e-12)
+    pt = m.nodes[:, m.boundary[TAG_PATCH]]
+    assert np.all(np.abs(pt[2] - 1.52e-3) < 1e-12)
+    assert np.all(np.abs(pt[0]) <= 0.02 + 1e-12) and np.all(np.abs(pt[1]) <= 0.015 + 1e-12)
+    # sheet areas: 80 x 80 mm ground, 40 x 30 mm patch, 5 x 1.52 mm feed
+    def area(tags):
+        tv = m.boundary[tags]
+        a, b, c = m.nodes[:, tv[0]], m.nodes[:, tv[1]], m.nodes[:, tv[2]]
+        return 0.5 * np.linalg.norm(np.cross((b - a).T, (c - a).T), axis=1).sum()
+    assert abs(area(TAG_GROUND) - 0.08 ** 2) < 1e-12
+    assert abs(area(TAG_PATCH) - 0.04 * 0.03) < 1e-12
+    assert abs(area(TAG_FEED) - 0.005 * 1.52e-3) < 1e-15
+    # the sheets are interior faces (two tets each), the substrate fills the slab under the patch
+    for tag in (TAG_GROUND, TAG_PATCH, TAG_FEED):
+        ids = m.tri_ids(m.boundary[tag])
+        assert np.all(m.tri_to_tet[1, ids] >= 0)
+    sub = m.cell_tag == 1
+    cz = m.nodes[2][m.tets[:, sub]].mean(axis=0)
+    assert np.all((cz > 0) & (cz < 1.52e-3))
+    assert np.isclose(p.er[0, 0][sub], 3.38 * (1 - 0.0027j)).all()
+    # the feed's voltage line runs from ground to patch through the feed centre
+    feed = p.bcs[2]
+    mid, step = feed.integration_line(m)
+    assert np.allclose(mid[:2].T, [[-0.01, 0.0]] * 10) and np.allclose(step.sum(axis=1), [0, 0, 1.52e-3])
+    assert z.min() == -0.0375 and abs(z.max() - (1.52e-3 + 0.0375)) < 1e-12
