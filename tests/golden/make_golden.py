@@ -30,6 +30,7 @@ Fixtures:
                      voltage lines of define_lumped_port_integration_points
                      (fem/physics/edm/emfreq3d.py:366-389), SuperLU fields and the
                      voltage-integral S-parameters (emfreq3d.py:752-766)
+  frames.npz         Axis.construct_cs (fem/cs.py:63-70): the port frames of 18 face normals
   port_elements.npz  generalized_matrix_GQ (fem/physics/edm/nedeleclegrange2.py:224-382), the
                      14x14 element matrices of the 2-D port mode problem, on 24 triangles with
                      random edge orientations and isotropic / anisotropic materials
@@ -425,6 +426,17 @@ def make_lumped():
     np.savez_compressed(os.path.join(HERE, "lumped.npz"), **out)
 
 
+def make_frames():
+    """Port frames the reference builds from a face normal (Axis.construct_cs, fem/cs.py:63-70)."""
+    from fem.cs import Axis
+    rng = np.random.default_rng(8)
+    normals = np.concatenate([np.eye(3), -np.eye(3), rng.normal(size=(10, 3)),
+                              [[0.9995, 0.01, 0.0], [1.0, 1e-4, 0.0]]])
+    bases = np.stack([Axis(n).construct_cs()._basis for n in normals])
+    np.savez_compressed(os.path.join(HERE, "frames.npz"), normals=normals, bases=bases)
+    print(f"frames: {len(normals)} normals")
+
+
 def make_port_elements():
     from fem.physics.edm import nedeleclegrange2 as ref_nl
     rng = np.random.default_rng(77)
@@ -519,7 +531,8 @@ def make_farfield():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc", "interp", "lumped", "port", "farfield"]
+    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc", "interp", "lumped", "frames", "port",
+                             "farfield"]
     if "tet" in which:
         make_tet_elements()
     if "tri" in which:
@@ -534,6 +547,8 @@ if __name__ == "__main__":
         make_interp()
     if "lumped" in which:
         make_lumped()
+    if "frames" in which:
+        make_frames()
     if "port" in which:
         make_port_elements()
     if "farfield" in which:

@@ -100,3 +100,11 @@ def test_line_weights_equal_interpolated_voltage(cuda):
             V = np.sum(Ex * step[0] + Ey * step[1] + Ez * step[2])
             Vw = np.sum(w * x[dofs])
             assert abs(Vw - V) <= 1e-12 * np.sum(np.abs(w * x[dofs]))
+
+
+def test_port_frames_match_reference():
+    """frame_from_normal against the reference's Axis.construct_cs (fem/cs.py:63-70)."""
+    from emerge_gb300.bc import frame_from_normal
+    z = load("frames.npz")
+    for n, B in zip(z["normals"], z["bases"]):
+        assert np.allclose(frame_from_normal(n)._basis, B, rtol=0, atol=1e-15), n
