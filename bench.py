@@ -10,13 +10,19 @@ mesh before timing (reported separately as ``plan_s``).  ``value``: tets/s with
 inputs resident in HBM (each step writes 27.5 GB of values, far more than the 129 MB
 L2, so no L2 flush is needed).  ``e2e``: the same through the C-ABI host entry point
 (emg_assemble_tet_host), with the material H2D and the E/B D2H inside the timed
-region.  ``--impl reference`` times the reference's CPU algorithm (the oracle's C++
+region; with the bench's page-locked outputs the fill stores straight into them.
+``--impl reference`` times the reference's CPU algorithm (the oracle's C++
 restatement of the Numba element loop on all host cores + SciPy
-coo_matrix(...).tocsr()) on a bounded sample of the same workload.
+coo_matrix(...).tocsr()) on a bounded sample of the same workload.  Under torchrun
+(N > 1) every rank assembles its own copy (replicas, weak scaling); the time is the
+slowest rank's.
 
-Sweep (``sweep``): the five-cavity iris filter, 401 points over 8-12 GHz x 2 ports,
-the batched mixed-precision warm-started GPU sweep against the plain FP64 GPU solver
-(see run_sweep).  Eigen (``eigen``): cavity eigenmodes (see run_eigen).
+Also reported: ``topology`` (the mesh's edge/face topology and DOF map on the GPU
+against the NumPy host build), ``farfield`` (Stratton-Chu transform against its FP32
+compute roofline and the NumPy restatement), ``sweep`` (the five-cavity iris filter,
+401 points over 8-12 GHz x 2 ports: the batched mixed-precision warm-started GPU sweep
+against the plain FP64 GPU solver, with the MLP and cold variants; see run_sweep) and
+``eigen`` (cavity eigenmodes against ARPACK; see run_eigen).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--n 80] [--impl reference]
                   [--no-sweep] [--sweep-h 2e-3] [--eigen 2] [--sweep-only] [--eigen-only]
