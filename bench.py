@@ -601,9 +601,9 @@ def main():
     ap.add_argument("--no-sweep", action="store_true", help="skip the frequency-sweep measurement")
     ap.add_argument("--sweep-h", type=float, default=2e-3, help="iris-filter mesh size (m)")
     ap.add_argument("--sweep-points", type=int, default=401)
-    ap.add_argument("--sweep-train", type=int, default=16, help="points solved first; their span gives the guesses")
+    ap.add_argument("--sweep-train", type=int, default=12, help="points solved first; their span gives the guesses")
     ap.add_argument("--sweep-mlp-train", type=int, default=32, help="training points of the MLP variant")
-    ap.add_argument("--sweep-anchors", type=int, default=4)
+    ap.add_argument("--sweep-anchors", type=int, default=2)
     ap.add_argument("--sweep-restart", type=int, default=40)
     ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: as many as fit ~80 GB)")
     ap.add_argument("--sweep-mlp-steps", type=int, default=300)
