@@ -649,10 +649,13 @@ void free_plan(emg_plan* p) {
     delete p;
 }
 
-bool g_vcoef_ready = false;
+// __constant__ memory is per device: the table is uploaded once for every device used
+bool g_vcoef_ready[64] = {false};
 
 int upload_vcoef() {
-    if (g_vcoef_ready) return EMG_OK;
+    int dev = 0;
+    EMG_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && g_vcoef_ready[dev]) return EMG_OK;
     static const double fact[10] = {1, 1, 2, 6, 24, 120, 720, 5040, 40320, 362880};
     double h[625];
     for (int a = 0; a < 5; ++a)
@@ -665,7 +668,7 @@ int upload_vcoef() {
                     h[((a * 5 + b) * 5 + c) * 5 + d] = num / fact[k[1] + k[2] + k[3] + k[4] + 3];
                 }
     EMG_CUDA(cudaMemcpyToSymbol(emg::c_vcoef, h, sizeof(h)));
-    g_vcoef_ready = true;
+    if (dev >= 0 && dev < 64) g_vcoef_ready[dev] = true;
     return EMG_OK;
 }
 
