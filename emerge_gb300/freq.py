@@ -115,32 +115,39 @@ class Assembler:
     def __init__(self, device: str | torch.device = "cuda"):
         self.cached_matrices = None
         self.device = torch.device(device)
-        self._dev = None           # (field id, plan, E, B)
-        self._robin = {}           # (field id, tags) -> _RobinPlan
-        self._solve_ids = {}       # (field id, pec tags) -> solve_ids
+        # caches hold the field (and material arrays) they were built for, so an id is
+        # never reused by another object while its entry lives
+        self._dev = None           # (field, er, ur, plan, E, B)
+        self._robin = {}           # (field id, tags) -> (field, _RobinPlan)
+        self._solve_ids = {}       # (field id, pec tags) -> (field, solve_ids)
         self._dpts = dunavant6()
         self._dpts_dev = None
 
     # ---------------------------------------------------------------- volume ---
     def _volume(self, field, er, ur):
-        key = id(field)
-        if self._dev is None or self._dev[0] != key:
+        """Device E and B of ``field`` for these material arrays (assembled again when
+        either the field or a material array is a different object)."""
+        d = self._dev
+        if d is None or d[0] is not field or d[1] is not er or d[2] is not ur:
             plan = plan_for(field, self.device)
             E, B = plan.assemble_materials(er, ur)
-            self._dev = (key, plan, E, B)
-        return self._dev[1], self._dev[2], self._dev[3]
+            self._dev = (field, er, ur, plan, E, B)
+        return self._dev[3], self._dev[4], self._dev[5]
 
     def _robin_plan(self, field, plan, bc):
         key = (id(field), tuple(bc.tags))
-        if key not in self._robin:
-            self._robin[key] = _RobinPlan(field, plan, field.mesh.get_triangles(bc.tags))
-        return self._robin[key]
+        hit = self._robin.get(key)
+        if hit is None or hit[0] is not field:
+            hit = (field, _RobinPlan(field, plan, field.mesh.get_triangles(bc.tags)))
+            self._robin[key] = hit
+        return hit[1]
 
     def solve_ids(self, field, bcs) -> np.ndarray:
         """DOFs not on PEC faces: 2 per PEC-face edge, 2 per PEC face (assembler.py:348-359, 384-385)."""
         pecs = [bc for bc in bcs if is_pec(bc)]
         key = (id(field), tuple(t for bc in pecs for t in bc.tags))
-        if key not in self._solve_ids:
+        hit = self._solve_ids.get(key)
+        if hit is None or hit[0] is not field:
             m = field.mesh
             N = field.n_field
             mask = np.ones(N, dtype=bool)
@@ -151,8 +158,9 @@ class Assembler:
                 edge_ids = np.asarray(m.tri_to_edge, dtype=np.int64)[:, tri_ids].ravel()
                 mask[np.asarray(field.edge_to_field, dtype=np.int64)[:, edge_ids].ravel()] = False
                 mask[np.asarray(field.tri_to_field, dtype=np.int64)[:, tri_ids].ravel()] = False
-            self._solve_ids[key] = np.flatnonzero(mask).astype(np.int64)
-        return self._solve_ids[key]
+            hit = (field, np.flatnonzero(mask).astype(np.int64))
+            self._solve_ids[key] = hit
+        return hit[1]
 
     # ---------------------------------------------------------- per frequency ---
     def device_system(self, field, er, ur, bcs, frequency: float) -> DeviceSystem:
@@ -219,12 +227,12 @@ class Assembler:
         """Drop-in for fem/physics/edm/assembler.py:312-388 -> (K, b, solve_ids, port_vectors) on the host."""
         from scipy.sparse import csr_matrix
         sysd = self.device_system(field, er, ur, bcs, frequency)
-        plan = self._dev[1]
+        plan = self._dev[3]
         ip, ix = plan.pattern_host()
         N = plan.n_field
         K = csr_matrix((sysd.K.cpu().numpy(), ix, ip), shape=(N, N))
         if cache_matrices and self.cached_matrices is None:
-            E, B = self._dev[2], self._dev[3]
+            E, B = self._dev[4], self._dev[5]
             self.cached_matrices = (csr_matrix((E.cpu().numpy(), ix, ip), shape=(N, N)),
                                     csr_matrix((B.cpu().numpy(), ix, ip), shape=(N, N)))
         b = np.zeros(N, dtype=np.complex128)

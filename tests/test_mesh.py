@@ -143,3 +143,31 @@ def test_patch_antenna_geometry():
     mid, step = feed.integration_line(m)
     assert np.allclose(mid[:2].T, [[-0.01, 0.0]] * 10) and np.allclose(step.sum(axis=1), [0, 0, 1.52e-3])
     assert z.min() == -0.0375 and abs(z.max() - (1.52e-3 + 0.0375)) < 1e-12
+
+
+def test_assembler_caches_follow_objects(monkeypatch):
+    """Assembler caches are keyed on the field and material objects themselves."""
+    import types
+    from emerge_gb300 import freq
+    built = []
+
+    class FakePlan:
+        def assemble_materials(self, er, ur):
+            built.append((er, ur))
+            return f"E{len(built)}", f"B{len(built)}"
+
+    monkeypatch.setattr(freq, "plan_for", lambda field, device: FakePlan())
+    monkeypatch.setattr(freq, "_RobinPlan", lambda field, plan, tris: ("robin", id(field), len(tris)))
+    asm = freq.Assembler(device="cpu")
+    f1 = types.SimpleNamespace(mesh=types.SimpleNamespace(get_triangles=lambda tags: np.arange(3)))
+    er, ur = np.ones((3, 3, 2)), np.ones((3, 3, 2))
+    p, E, B = asm._volume(f1, er, ur)
+    assert (E, B) == ("E1", "B1")
+    assert asm._volume(f1, er, ur)[1] == "E1" and len(built) == 1          # same objects: cached
+    assert asm._volume(f1, er.copy(), ur)[1] == "E2"                       # new material array
+    f2 = types.SimpleNamespace(mesh=f1.mesh)
+    assert asm._volume(f2, er, ur)[1] == "E3"                              # new field
+    bc = types.SimpleNamespace(tags=[1])
+    r1 = asm._robin_plan(f1, p, bc)
+    assert asm._robin_plan(f1, p, bc) is r1
+    assert asm._robin_plan(f2, p, bc) is not r1
