@@ -40,10 +40,14 @@ def unpack(w: np.ndarray, K, N):
     return Ws, bs
 
 
-def forward_backward(w, x, t, in_dim, hidden, layers, out_dim):
-    """Returns (output (nb, out_dim), loss, flat gradient) of the GPU training step."""
+def forward_backward(w, x, t, in_dim, hidden, layers, out_dim, rounding: bool = True):
+    """Returns (output (nb, out_dim), loss, flat gradient) of the GPU training step.
+
+    rounding=False drops the bf16 roundings (and the float32 weights): the exact FP64
+    loss and gradient, which a finite-difference test checks the backward formulas on."""
+    bf16 = globals()["bf16"] if rounding else (lambda a: np.asarray(a, dtype=np.float64))
     K, N = layer_dims(in_dim, hidden, layers, out_dim)
-    Ws, bs = unpack(np.asarray(w, dtype=np.float32), K, N)
+    Ws, bs = unpack(np.asarray(w, dtype=np.float32 if rounding else np.float64), K, N)
     nb = x.shape[0]
     R = pad16(nb)
     H0 = np.zeros((R, K[0]))

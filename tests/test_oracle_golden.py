@@ -99,3 +99,25 @@ def test_vectorised_matinv_matches_oracle():
     for t in range(nT):
         ref = oracle.matinv(s[:, :, t])
         assert np.allclose(got[:, :, t], ref, rtol=1e-14, atol=0)
+
+
+def test_mlp_oracle_gradient_by_finite_differences():
+    """The MLP oracle's backward pass (the checker of the GPU training kernels) against
+    central differences of its own loss, in FP64 without the bf16 roundings."""
+    from oracle import mlp_oracle as mo
+    rng = np.random.default_rng(0)
+    in_dim, hidden, layers, out_dim, nb = 3, 16, 2, 5, 7
+    K, N = mo.layer_dims(in_dim, hidden, layers, out_dim)
+    npar = sum(n * k + n for k, n in zip(K, N))
+    w = rng.normal(size=npar) * 0.3
+    x = rng.normal(size=(nb, in_dim))
+    t = rng.normal(size=(nb, out_dim))
+    _, _, g = mo.forward_backward(w, x, t, in_dim, hidden, layers, out_dim, rounding=False)
+    # only parameters that reach the loss (padding rows/columns carry zero gradient)
+    for i in rng.choice(npar, 60, replace=False):
+        e = np.zeros(npar)
+        e[i] = 1e-6
+        lp = mo.forward_backward(w + e, x, t, in_dim, hidden, layers, out_dim, rounding=False)[1]
+        lm = mo.forward_backward(w - e, x, t, in_dim, hidden, layers, out_dim, rounding=False)[1]
+        fd = (lp - lm) / 2e-6
+        assert abs(fd - g[i]) <= 1e-7 + 1e-6 * abs(g[i]), (i, fd, g[i])
