@@ -171,3 +171,37 @@ def test_assembler_caches_follow_objects(monkeypatch):
     r1 = asm._robin_plan(f1, p, bc)
     assert asm._robin_plan(f1, p, bc) is r1
     assert asm._robin_plan(f2, p, bc) is not r1
+
+
+def test_sparameters_of_mixed_port_types():
+    """FrequencySweep._sparams with a waveport and a lumped port: S_ij = pfield_i / pmode_j
+    with each port's own formula (fem/physics/edm/emfreq3d.py:735-766, fem/mth/sparam.py)."""
+    import types
+    import torch
+    from emerge_gb300.solver import FrequencySweep
+    rng = np.random.default_rng(4)
+    n, nf = 40, 3
+    wave = types.SimpleNamespace(port_number=1, Zmode=lambda k0: 376.73)
+    lump = types.SimpleNamespace(port_number=2, v_integration=True, integration_line=None, voltage=10.0, Z0=50.0)
+    sw = object.__new__(FrequencySweep)
+    sw.ports = [wave, lump]
+    u = rng.normal(size=(n, 2)) + 1j * rng.normal(size=(n, 2))
+    sw.u_r = torch.as_tensor(u)
+    sw.Pmode = np.array([2.5, 0.0])
+    r = torch.as_tensor(rng.choice(n, 6, replace=False))
+    w = torch.as_tensor(rng.normal(size=6) + 0j)
+    sw._vfun = {1: (r, w)}
+    X = rng.normal(size=(n, nf * 2)) + 1j * rng.normal(size=(n, nf * 2))
+    k0 = np.array([100.0, 150.0, 200.0])
+    S = sw._sparams(torch.as_tensor(X), nf, np.ones((2, nf)), k0)
+    V0, Z0, P = 10.0, 50.0, 2.5
+    for f in range(nf):
+        for j in range(2):
+            c = f * 2 + j
+            pm = P / (2 * 376.73) if j == 0 else np.sqrt(V0 ** 2 / (2 * Z0))
+            G = -(u[:, 0] @ X[:, c])
+            V = np.sum(w.numpy() * X[r.numpy(), c])
+            pf = [(G - (P if j == 0 else 0.0)) / (2 * 376.73),
+                  np.sqrt((V - (V0 if j == 1 else 0.0)) ** 2 / (2 * Z0))]
+            for i in range(2):
+                assert np.isclose(S[f, i, j], pf[i] / pm, rtol=1e-12, atol=0)
