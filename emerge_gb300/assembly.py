@@ -114,6 +114,9 @@ class AssemblyPlan:
         def f64(a):
             return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)
 
+        # the arrays this plan was built from: a field whose mesh arrays were
+        # replaced (moved nodes, a new mesh of the same size) gets a new plan
+        self._source = (m.nodes, m.tets, m.edges, m.tris, field.tet_to_field)
         self.n_tets = int(m.tets.shape[1])
         self.n_edges = int(m.edges.shape[1])
         self.n_tris = int(m.tris.shape[1])
@@ -138,6 +141,12 @@ class AssemblyPlan:
         with torch.cuda.device(dev):
             _lib.call("emg_plan_pattern", plan, _dptr(self.indptr), _dptr(self.indices), _stream())
         self._host_pattern = None
+
+    def matches(self, field) -> bool:
+        """True when ``field`` still holds the very arrays this plan was built from."""
+        m = field.mesh
+        now = (m.nodes, m.tets, m.edges, m.tris, field.tet_to_field)
+        return all(a is b for a, b in zip(self._source, now))
 
     @staticmethod
     def n_nodes_of(m) -> int:
@@ -231,7 +240,7 @@ class AssemblyPlan:
 def plan_for(field, device: str | torch.device = "cuda") -> AssemblyPlan:
     """The cached plan of ``field`` (built on first use)."""
     plan = getattr(field, "_emg_assembly_plan", None)
-    if plan is None or plan.n_tets != field.mesh.tets.shape[1]:
+    if plan is None or not plan.matches(field):
         plan = AssemblyPlan(field, device)
         try:
             field._emg_assembly_plan = plan

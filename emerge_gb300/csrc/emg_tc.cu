@@ -10,8 +10,10 @@
 //     overwrites the staging buffers;
 //   - the accumulator (128 lanes x 64 columns of TMEM) is read back with
 //     tcgen05.ld.32x32b (warp w reads lanes 32w..32w+31) and stored.
-// Every wait is bounded: on timeout the CTA records an error in *status, skips the
-// remaining work, and still frees its TMEM.
+// Every wait is bounded: on timeout the CTA records an error in *status, gives the
+// MMAs it already committed one more bounded wait, skips the remaining work, and still
+// frees its TMEM.  After a nonzero status the host discards the output tile and does
+// not relaunch on the same data.
 #include "emg_krylov.cuh"
 
 namespace emg {
@@ -19,7 +21,11 @@ namespace tc {
 
 constexpr int kM = 128, kN = 64, kK = 32, kThreads = 128;
 constexpr uint32_t kTmemCols = 64;
-constexpr long long kSpinLimit = 1ll << 16;   // a chunk's MMAs finish in well under a microsecond
+// Waits on an mbarrier end after kWaitNs of wall time (the chunk's MMAs finish in well
+// under a microsecond, so only a lost arrival gets there), polled with a short sleep so a
+// busy SM does not time out early; kSpinLimit caps the polls as a second bound.
+constexpr unsigned long long kWaitNs = 10ull * 1000ull * 1000ull;   // 10 ms
+constexpr long long kSpinLimit = 1ll << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -43,7 +49,14 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    const unsigned long long t0 = global_ns();
     for (long long it = 0; it < kSpinLimit; ++it) {
         uint32_t done = 0;
         asm volatile(
@@ -54,6 +67,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
             : "r"(mbar), "r"(phase)
             : "memory");
         if (done) return true;
+        if ((it & 63) == 63) {
+            if (global_ns() - t0 > kWaitNs) return false;
+            __nanosleep(256);
+        }
     }
     return false;
 }

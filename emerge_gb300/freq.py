@@ -163,7 +163,10 @@ class Assembler:
         return hit[1]
 
     # ---------------------------------------------------------- per frequency ---
-    def device_system(self, field, er, ur, bcs, frequency: float) -> DeviceSystem:
+    def device_system(self, field, er, ur, bcs, frequency: float, force_weights: dict | None = None) -> DeviceSystem:
+        """K(k0), port vectors and solve_ids on the device.  ``force_weights`` maps a port
+        number to one complex weight per port triangle that scales its U_inc (used for the
+        material-weighted S-parameter functionals of the sweep)."""
         plan, E, B = self._volume(field, er, ur)
         dev = self.device
         k0 = 2 * np.pi * frequency / C0
@@ -197,6 +200,8 @@ class Assembler:
                 y = (lcs[1][:, None, :] * D[1:, :, None]).sum(axis=0)
                 # generate_points order: (npts, n) flattened (assembler.py:63-81)
                 U = np.asarray(bc.get_Uinc(x.ravel(), y.ravel(), k0), dtype=np.complex128).reshape(3, D.shape[1], rp.n)
+                if force_weights and bc.port_number in force_weights:
+                    U = U * np.asarray(force_weights[bc.port_number], dtype=np.complex128)[None, None, :]
                 lcs_d = torch.as_tensor(lcs, device=dev)
                 U_d = torch.as_tensor(np.ascontiguousarray(U), device=dev)
                 bblk = torch.empty(rp.n * 8, dtype=torch.complex128, device=dev)

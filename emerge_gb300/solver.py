@@ -338,6 +338,16 @@ class SlabFactor:
         return x, its.cpu().numpy(), res.cpu().numpy()
 
 
+def pattern_key(A) -> tuple:
+    """Cache key of a CSR pattern: shape, nnz and a hash of the whole indptr and indices.
+
+    Two patterns with equal row lengths and equal leading columns must not share a
+    key (a renumbered mesh of the same structure), so every column index is hashed;
+    this is O(nnz) host work, small next to a factorization.
+    """
+    return (A.shape[0], A.shape[1], int(A.nnz), hash(A.indptr.tobytes()), hash(A.indices.tobytes()))
+
+
 class GPUSolver:
     """``Solver`` for the reference SolveRoutine (fem/solver.py:117-131) on the GPU.
 
@@ -379,7 +389,7 @@ class GPUSolver:
         A = csr_matrix(A)
         A.sort_indices()
         n = A.shape[0]
-        key = (n, A.nnz, hash(A.indices[: min(A.nnz, 4096)].tobytes()), hash(A.indptr.tobytes()))
+        key = pattern_key(A)
         dev = self.device
         if key != self._key:
             indptr = torch.as_tensor(A.indptr.astype(np.int64), device=dev)
@@ -468,11 +478,34 @@ class FrequencySweep:
         self.solve_ids = sysd.solve_ids
         self.sys = RestrictedSystem(plan.indptr, plan.indices[: plan.nnz], plan.nnz, self.solve_ids)
         self.u_r = self.sys.gather(torch.stack([self.u[bc.port_number] for bc in self.ports]))   # (n, np)
-        self.Pmode = np.array([_mode_power(field, bc) for bc in self.ports])
+        # per waveport triangle, the material weight of its mode integrals (emfreq3d.py:767-778);
+        # the S-parameter functionals u_w carry it, the forcing u_r does not
+        self.sconst = [None if _is_lumped(bc) else _port_const(field, bc, er, ur) for bc in self.ports]
+        self.u_w = self._weighted_functionals(assembler, field, er, ur, unit_bcs)
+        self.Pmode = np.array([_mode_power(field, bc, c) for bc, c in zip(self.ports, self.sconst)])
         # forcing amplitude per unit port mode: U_inc = -2j beta amp E_mode (1 for waveports,
         # whose mode carries its amplitude; V/h * 376.7303/Zs for lumped ports)
         self.amp = np.array([_lumped_amp(bc) if _is_lumped(bc) else 1.0 for bc in self.ports])
         self._vfun = self._voltage_functionals()
+
+    def _weighted_functionals(self, assembler, field, er, ur, unit_bcs):
+        """(n, np) restricted functionals G_i(x) = -u_w,i . x = int const E . E_mode_i.
+
+        A port whose faces carry one material weight c gets c * u_i; a port with
+        mixed fills gets its forcing vector assembled again with U_inc scaled by
+        each triangle's weight."""
+        cols = []
+        for i, bc in enumerate(self.ports):
+            c = self.sconst[i]
+            if c is None or len(c) == 0 or np.all(c == c[0]):
+                w = 1.0 if c is None or len(c) == 0 else complex(c[0])
+                cols.append(self.u_r[:, i] * w)
+                continue
+            solo = [b for b in unit_bcs if not isinstance(b, _UnitRobin) or b.bc is bc]
+            sw = assembler.device_system(field, er, ur, solo, frequency=C0 / (2 * np.pi),
+                                         force_weights={bc.port_number: c})
+            cols.append(self.sys.gather(sw.port_vectors[bc.port_number].reshape(1, -1))[0])
+        return torch.stack(cols, dim=1)
 
     def _voltage_functionals(self):
         """Per lumped port, its line voltage sum_i E(mid_i) . dl_i as a sparse functional of
@@ -525,7 +558,7 @@ class FrequencySweep:
         Lumped ports (emfreq3d.py:752-766): V = line voltage, pfield = sqrt((V - [i = j] V0)^2
         / (2 Z0)), pmode = sqrt(V0^2 / (2 Z0)), principal square roots as the reference."""
         npo = len(self.ports)
-        G = -(self.u_r.T @ X).cpu().numpy()                                                      # (np, nf*np)
+        G = -(self.u_w.T @ X).cpu().numpy()                                                      # (np, nf*np)
         V = {i: (w[:, None] * X[r]).sum(dim=0).cpu().numpy() for i, (r, w) in self._vfun.items()}
         S = np.zeros((nf, npo, npo), dtype=np.complex128)
         for f in range(nf):
@@ -924,8 +957,27 @@ def _zmode(bc, k0) -> float:
     return complex(z(k0)) if callable(z) else 376.730313412
 
 
-def _mode_power(field, bc) -> float:
-    """int |E_mode|^2 over the port face with the 6-point rule (fem/mth/sparam.py:72-100)."""
+def _port_const(field, bc, er, ur) -> np.ndarray:
+    """Per port triangle, the weight of the S-parameter mode integrals
+    (fem/physics/edm/emfreq3d.py:767-778): TEM sqrt(tr er / tr ur), TE 3 / tr ur,
+    TM 3 / tr er, with the material of the face's first tet (emfreq3d.py:480-486)."""
+    m = field.mesh
+    tri = np.asarray(m.get_triangles(bc.tags), dtype=np.int64)
+    tet = np.asarray(m.tri_to_tet, dtype=np.int64)[0, tri]
+    er = np.asarray(er)
+    ur = np.asarray(ur)
+    tre = er[0, 0, tet] + er[1, 1, tet] + er[2, 2, tet]
+    tru = ur[0, 0, tet] + ur[1, 1, tet] + ur[2, 2, tet]
+    kind = getattr(bc, "modetype", "TEM")
+    if kind == "TE":
+        return (1.0 / (tru / 3)).astype(np.complex128)
+    if kind == "TM":
+        return (1.0 / (tre / 3)).astype(np.complex128)
+    return (1.0 / np.sqrt(tru / tre)).astype(np.complex128)
+
+
+def _mode_power(field, bc, const=None) -> complex:
+    """int const |E_mode|^2 over the port face with the 6-point rule (fem/mth/sparam.py:72-100)."""
     from .freq import dunavant6
     m = field.mesh
     tri = np.asarray(m.get_triangles(bc.tags), dtype=np.int64)
@@ -938,5 +990,6 @@ def _mode_power(field, bc) -> float:
     for k in range(D.shape[1]):
         p = v1 * D[1, k] + v2 * D[2, k] + v3 * D[3, k]
         Em = bc.port_mode_3d_global(p[0], p[1], p[2], 1.0)
-        tot += D[0, k] * np.sum(np.sum(np.abs(Em) ** 2, axis=0) * area)
-    return float(tot)
+        w = area if const is None else area * const
+        tot += D[0, k] * np.sum(np.sum(np.abs(Em) ** 2, axis=0) * w)
+    return float(tot) if const is None else complex(tot)

@@ -303,7 +303,8 @@ int emg_gmres_slab_family(const emg_rplan* plan, emg_slab* slab, int64_t Bc, int
  * accumulation in tensor memory): A (M x K, ld lda), B (N x K, ld ldb), D (M x N,
  * ld ldd), row-major FP32 DEVICE arrays; TF32 products (10-bit mantissa).
  * *status (DEVICE int32, set to 0 by the caller) becomes 1 if a tile's bounded
- * wait on its tensor-core work ran out. */
+ * wait (10 ms) on its tensor-core work ran out; D is then invalid and the caller
+ * discards it rather than relaunching on the same data. */
 int emg_tc_gemm_tf32(int64_t M, int64_t N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
                      float* D, int64_t ldd, int32_t* status, void* stream);
 
@@ -337,7 +338,9 @@ void emg_mlp_destroy(emg_mlp* mlp);
  * return EMG_ERR_LIMIT).  Inputs and outputs are caller-owned DEVICE arrays:
  * tet_to_field (20, n_tets) int32, indptr (n_field+1) int64, indices
  * (indices_capacity) int32; *nnz_out (host) receives nnz, and EMG_ERR_LIMIT is
- * returned when nnz > indices_capacity.  The scratch is one ~4.9 MB device array
+ * returned when nnz > indices_capacity.  After that capacity shortfall *nnz_out
+ * and indptr are already valid (indices is not written), so the caller can size
+ * indices from *nnz_out and call again.  The scratch is one ~4.9 MB device array
  * in the library, held by every GPU that loads it until the process exits; the
  * first call on a device looks up its address.  All calls share that array, so
  * calls that overlap on the GPU (other streams or host threads) race.

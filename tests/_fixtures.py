@@ -19,6 +19,8 @@ def field_from(z) -> types.SimpleNamespace:
     mesh = types.SimpleNamespace(nodes=np.asarray(z["nodes"]), tets=i8("tets"), tris=i8("tris"), edges=i8("edges"),
                                  edge_lengths=np.asarray(z["edge_lengths"]), tet_to_edge=i8("tet_to_edge"),
                                  tet_to_tri=i8("tet_to_tri"), tri_to_edge=i8("tri_to_edge"))
+    if "tri_to_tet" in z:
+        mesh.tri_to_tet = i8("tri_to_tet")
     mesh.n_tets = mesh.tets.shape[1]
     mesh.n_edges = mesh.edges.shape[1]
     mesh.n_tris = mesh.tris.shape[1]

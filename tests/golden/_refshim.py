@@ -18,12 +18,15 @@ The ``fem`` packages are registered as namespace modules so that
 """
 from __future__ import annotations
 
+import os
 import sys
 import types
 
 import numpy as np
 
-REF_ROOT = "/root/reference"
+# Root of the EMerge checkout (the directory holding ``fem/``): set by
+# ``make_golden.py --ref PATH`` or the EMERGE_REF_ROOT environment variable.
+REF_ROOT = os.environ.get("EMERGE_REF_ROOT", "")
 
 
 class _AnyType:
@@ -153,6 +156,9 @@ class FakeGmsh(types.ModuleType):
 
 def install() -> FakeGmsh:
     """Register every stand-in and the ``fem`` namespace packages; return the fake gmsh."""
+    if not REF_ROOT or not os.path.isdir(os.path.join(REF_ROOT, "fem")):
+        raise RuntimeError("the EMerge checkout is not set: pass --ref PATH to make_golden.py "
+                           "or set EMERGE_REF_ROOT to the directory that holds fem/")
     _install_numba()
     _install_loguru()
     g = FakeGmsh()

@@ -1,8 +1,10 @@
 """Generate the golden fixtures in tests/golden/ by running the EMerge reference.
 
-Run in a checkout that has the reference at /root/reference:
+Run with the path of an EMerge checkout (the directory that holds ``fem/``):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --ref /root/reference [fixture ...]
+
+(or set EMERGE_REF_ROOT instead of passing ``--ref``).
 
 The reference runs unmodified behind the import shims of ``_refshim`` (Numba
 kernels execute as plain Python, gmsh is replaced by a fake that serves the
@@ -34,6 +36,11 @@ Fixtures:
   port_elements.npz  generalized_matrix_GQ (fem/physics/edm/nedeleclegrange2.py:224-382), the
                      14x14 element matrices of the 2-D port mode problem, on 24 triangles with
                      random edge orientations and isotropic / anisotropic materials
+  waveguide_k.npz    K(k0) of the waveguide at 10 GHz entry by entry on the port-face rows
+                     and 1500 random rows (fem/physics/edm/assembler.py:312-388)
+  waveguide_diel.npz the guide with a lossy dielectric at port 1: SuperLU fields and the
+                     S-parameters with the per-triangle material weight of the mode
+                     integrals (fem/physics/edm/emfreq3d.py:767-778)
   farfield.npz       stratton_chu (fem/physics/edm/sc.py:143-180) of a short dipole's
                      near field sampled at the edge centres of a closed box surface
 """
@@ -51,6 +58,12 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import _refshim  # noqa: E402
 
+# ``--ref PATH``: the EMerge checkout to run (else EMERGE_REF_ROOT)
+_ARGS = sys.argv[1:]
+if "--ref" in _ARGS:
+    _i = _ARGS.index("--ref")
+    _refshim.REF_ROOT = _ARGS[_i + 1]
+    del _ARGS[_i:_i + 2]
 GMSH = _refshim.install()
 
 from fem.mth import tet as ref_tet  # noqa: E402
@@ -277,6 +290,108 @@ def make_waveguide():
     out["S"] = S
     out["port_tets"] = port_tets.astype(np.int32)
     np.savez_compressed(os.path.join(HERE, "waveguide.npz"), **out)
+
+
+def _guide_ports(m, a, b, L):
+    p1 = ref_bc.RectangularWaveguide(FaceSelection([pm.FACE_YMIN]), 1, cs=CoordinateSystem(
+        Axis(np.array([1.0, 0, 0])), Axis(np.array([0, 0, 1.0])), Axis(np.array([0, -1.0, 0])),
+        np.array([a / 2, 0.0, b / 2])), dims=(a, b))
+    p2 = ref_bc.RectangularWaveguide(FaceSelection([pm.FACE_YMAX]), 2, cs=CoordinateSystem(
+        Axis(np.array([-1.0, 0, 0])), Axis(np.array([0, 0, 1.0])), Axis(np.array([0, 1.0, 0])),
+        np.array([a / 2, L, b / 2])), dims=(a, b))
+    p1.dims = (a, b)
+    p2.dims = (a, b)
+    for p in (p1, p2):
+        p._tri_ids = m.get_triangles(p.tags)
+        p._tri_vertices = m.tris[:, p._tri_ids]
+    pec = ref_bc.PEC(FaceSelection([pm.FACE_XMIN, pm.FACE_XMAX, pm.FACE_ZMIN, pm.FACE_ZMAX]))
+    return p1, p2, pec
+
+
+def make_waveguide_k():
+    """Entry-by-entry K(k0) of the WR-90 guide at 10 GHz (assembler.py:312-388) on a row
+    subset: every row of a port-face DOF (where the Robin blocks land) plus 1500 random
+    rows.  The mesh is the one of waveguide.npz (checked)."""
+    tm, (a, b, L) = waveguide_mesh()
+    m = reference_mesh(tm)
+    ref = np.load(os.path.join(HERE, "waveguide.npz"))
+    assert np.array_equal(ref["tets"], m.tets) and np.array_equal(ref["edges"], m.edges)
+    assert np.array_equal(ref["tris"], m.tris)
+    field = Nedelec2(m)
+    nT = m.n_tets
+    er = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    ur = er.copy()
+    p1, p2, pec = _guide_ports(m, a, b, L)
+    asm = ref_assembler.Assembler()
+    f = 10.0e9
+    K, bvec, solve_ids, pvecs = asm.assemble_freq_matrix(field, er, ur, [pec, p1, p2], f, cache_matrices=True)
+    Kc = K.tocsr()
+    Kc.sort_indices()
+    rng = np.random.default_rng(11)
+    port_rows = np.unique(field.tri_to_field[:, np.r_[p1._tri_ids, p2._tri_ids]])
+    rows = np.unique(np.r_[port_rows, rng.choice(Kc.shape[0], 1500, replace=False)]).astype(np.int64)
+    sub = Kc[rows]
+    np.savez_compressed(os.path.join(HERE, "waveguide_k.npz"), freq=np.float64(f), rows=rows,
+                        port_rows=port_rows.astype(np.int64), indptr=sub.indptr.astype(np.int64),
+                        indices=sub.indices.astype(np.int32), data=sub.data, nnz_total=np.int64(Kc.nnz))
+    print(f"waveguide_k: {len(rows)} rows, {sub.nnz} entries of {Kc.nnz}")
+
+
+def make_waveguide_diel():
+    """WR-90 guide with its first 20 mm filled by a lossy dielectric (er = 2.2 - 0.02j), so the
+    two waveports see different fills: the S-parameters carry the reference's per-triangle
+    material weight of the mode integrals (emfreq3d.py:767-778, sparam.py:102-139), with the
+    port-face materials taken from each face's first tet (emfreq3d.py:480-486)."""
+    tm, (a, b, L) = waveguide_mesh()
+    m = reference_mesh(tm)
+    field = Nedelec2(m)
+    nT = m.n_tets
+    cy = m.nodes[1][m.tets].mean(axis=0)
+    eps = np.where(cy < 0.02, 2.2 - 0.02j, 1.0 + 0j)
+    er = np.eye(3, dtype=np.complex128)[:, :, None] * eps[None, None, :]
+    ur = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    p1, p2, pec = _guide_ports(m, a, b, L)
+    all_ports = [p1, p2]
+    ertri = er[:, :, m.tri_to_tet[0]]
+    urtri = ur[:, :, m.tri_to_tet[0]]
+    verts = set()
+    for p in all_ports:
+        verts.update(set(p._tri_vertices.ravel().tolist()))
+    port_tets = np.array([t for t in range(nT) if not set(m.tets[:, t].tolist()).isdisjoint(verts)])
+    asm = ref_assembler.Assembler()
+    routine = ref_solver.SolveRoutine(ref_solver.ReverseCuthillMckee(), ref_solver.Preconditioner(), None,
+                                      ref_solver.SolverSuperLU(), None, None)
+    routine.use_preconditioner = False
+    phys = Electrodynamics3D.__new__(Electrodynamics3D)
+    phys.mesh = m
+    f = 10.0e9
+    k0 = 2 * np.pi * f / C0
+    K, bvec, solve_ids, pvecs = asm.assemble_freq_matrix(field, er, ur, [pec, p1, p2], f, cache_matrices=True)
+    out = mesh_arrays(m)
+    out["tet_to_field"] = field.tet_to_field.astype(np.int32)
+    out["tri_to_field"] = field.tri_to_field.astype(np.int32)
+    out["dims"] = np.array([a, b, L])
+    out["freq"] = np.float64(f)
+    out["eps"] = eps
+    out["port_tris_1"] = p1._tri_ids.astype(np.int32)
+    out["port_tris_2"] = p2._tri_ids.astype(np.int32)
+    out["pec_tris"] = m.get_triangles(pec.tags).astype(np.int32)
+    S = np.zeros((2, 2), dtype=np.complex128)
+    for active in all_ports:
+        active.active = True
+        sol = routine.solve(K, bvec + pvecs[active.port_number], solve_ids, reuse=False)
+        out[f"x_{active.port_number}"] = sol
+        fieldf = field.interpolate_Ef(sol, tetids=port_tets)
+        tr = active._tri_ids
+        _, pmode = phys._compute_s_data(active, fieldf, active._tri_vertices, k0, ertri[:, :, tr], urtri[:, :, tr])
+        for bcp in all_ports:
+            tr = bcp._tri_ids
+            pf, _ = phys._compute_s_data(bcp, fieldf, bcp._tri_vertices, k0, ertri[:, :, tr], urtri[:, :, tr])
+            S[bcp.port_number - 1, active.port_number - 1] = pf / pmode
+        active.active = False
+    out["S"] = S
+    np.savez_compressed(os.path.join(HERE, "waveguide_diel.npz"), **out)
+    print(f"waveguide_diel: |S11|={abs(S[0, 0]):.4f} |S21|={abs(S[1, 0]):.4f} |S12|={abs(S[0, 1]):.4f}")
 
 
 def make_waveguide_abc():
@@ -531,8 +646,8 @@ def make_farfield():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["tet", "tri", "small", "waveguide", "abc", "interp", "lumped", "frames", "port",
-                             "farfield"]
+    which = _ARGS or ["tet", "tri", "small", "waveguide", "abc", "interp", "lumped", "frames", "port",
+                      "farfield", "waveguide_k", "waveguide_diel"]
     if "tet" in which:
         make_tet_elements()
     if "tri" in which:
@@ -553,3 +668,7 @@ if __name__ == "__main__":
         make_port_elements()
     if "farfield" in which:
         make_farfield()
+    if "waveguide_k" in which:
+        make_waveguide_k()
+    if "waveguide_diel" in which:
+        make_waveguide_diel()

@@ -121,3 +121,34 @@ def test_absorbing_boundary_matrix_matches_reference(torch_cuda):
     ref = np.zeros(n, dtype=np.complex128)
     ref[z["pvec_1_idx"]] = z["pvec_1_val"]
     assert np.max(np.abs(pvs[1] - ref)) <= TOL * np.max(np.abs(ref))
+
+
+def test_waveguide_k_entries_match_reference(torch_cuda):
+    """K(k0) at 10 GHz entry by entry against the reference's own K on the rows of the
+    port faces (where the Robin blocks land) and 1500 random rows.  The reference's
+    ``E - B*k0**2`` drops exact zeros (scipy binop), so every reference entry must be
+    found in our pattern within 1e-12 of its row's largest entry, and every entry of ours
+    outside the reference pattern must be exactly zero."""
+    from emerge_gb300.freq import Assembler
+    z = load("waveguide.npz")
+    k = load("waveguide_k.npz")
+    field, bcs = waveguide_field_and_bcs(z)
+    nT = field.mesh.n_tets
+    eye = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], nT, axis=2)
+    K, _, _, _ = Assembler().assemble_freq_matrix(field, eye, eye, bcs, float(k["freq"]))
+    K = K.tocsr()
+    rows, ip, ix, dv = k["rows"], k["indptr"], k["indices"], k["data"]
+    assert len(rows) > 2000 and len(np.intersect1d(rows, k["port_rows"])) == len(k["port_rows"])
+    worst = 0.0
+    for r_i, r in enumerate(rows):
+        ref_c, ref_v = ix[ip[r_i]:ip[r_i + 1]], dv[ip[r_i]:ip[r_i + 1]]
+        our_c = K.indices[K.indptr[r]:K.indptr[r + 1]]
+        our_v = K.data[K.indptr[r]:K.indptr[r + 1]]
+        pos = np.searchsorted(our_c, ref_c)
+        assert np.all(pos < len(our_c)) and np.array_equal(our_c[pos], ref_c), f"row {r}: pattern"
+        scale = max(np.abs(ref_v).max(), 1e-300)
+        worst = max(worst, float(np.abs(our_v[pos] - ref_v).max() / scale))
+        extra = np.ones(len(our_c), dtype=bool)
+        extra[pos] = False
+        assert not np.any(our_v[extra]), f"row {r}: nonzero entry outside the reference pattern"
+    assert worst <= TOL, worst

@@ -187,6 +187,7 @@ def test_sparameters_of_mixed_port_types():
     sw.ports = [wave, lump]
     u = rng.normal(size=(n, 2)) + 1j * rng.normal(size=(n, 2))
     sw.u_r = torch.as_tensor(u)
+    sw.u_w = sw.u_r
     sw.Pmode = np.array([2.5, 0.0])
     r = torch.as_tensor(rng.choice(n, 6, replace=False))
     w = torch.as_tensor(rng.normal(size=6) + 0j)

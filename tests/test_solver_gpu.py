@@ -127,3 +127,25 @@ def test_matrix_family_product_equals_formed_matrices(waveguide):
     ref = sw.sys.spmv(A, X, cm)
     got = sw.sys.spmv_family(fam, torch.as_tensor(coef, device="cuda"), X)
     assert (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item() <= 1e-13
+
+
+def test_dielectric_port_sparams_match_reference(torch_cuda):
+    """A guide whose port 1 face sits in a lossy dielectric (er = 2.2 - 0.02j) and port 2 in
+    air: the S-parameters carry the reference's per-triangle material weight of the mode
+    integrals (fem/physics/edm/emfreq3d.py:767-778), which makes |S12 / S21| close to |er1| here.
+    Sweep S against the reference's, fields against its SuperLU solutions."""
+    from emerge_gb300.freq import Assembler
+    from emerge_gb300.solver import FrequencySweep
+    z = load("waveguide_diel.npz")
+    field, bcs = waveguide_field_and_bcs(z)
+    er = np.eye(3, dtype=np.complex128)[:, :, None] * z["eps"][None, None, :]
+    ur = np.repeat(np.eye(3, dtype=np.complex128)[:, :, None], field.mesh.n_tets, axis=2)
+    sw = FrequencySweep(Assembler(), field, er, ur, bcs)
+    res = sw.run(np.array([float(z["freq"])]), method="plain", tol=1e-11)
+    assert np.all(res.residuals <= 1e-10)
+    X = sw.sys.scatter(res.solutions).cpu().numpy()
+    for p in range(2):
+        ref = z[f"x_{p + 1}"]
+        assert np.linalg.norm(X[p] - ref) / np.linalg.norm(ref) <= 1e-6
+    assert np.max(np.abs(res.S[0] - z["S"])) <= 1e-4
+    assert abs(abs(z["S"][0, 1] / z["S"][1, 0]) - abs(2.2 - 0.02j)) < 0.05
