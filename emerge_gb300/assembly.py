@@ -169,6 +169,18 @@ class AssemblyPlan:
             self._host_pattern = (ip.astype(idx_t), ix.astype(idx_t))
         return self._host_pattern
 
+    def rows_host(self, rows, *values: torch.Tensor):
+        """Rows ``rows`` of device CSR value arrays on this plan's pattern, copied to the host:
+        (indptr, indices, *values) of the (len(rows), N) row block."""
+        r = torch.as_tensor(np.asarray(rows, dtype=np.int64), device=self.device)
+        start, stop = self.indptr[r], self.indptr[r + 1]
+        cnt = stop - start
+        ip = torch.zeros(len(r) + 1, dtype=torch.int64, device=self.device)
+        ip[1:] = torch.cumsum(cnt, 0)
+        owner = torch.repeat_interleave(torch.arange(len(r), device=self.device), cnt)
+        pos = start[owner] + (torch.arange(int(ip[-1]), device=self.device) - ip[:-1][owner])
+        return (ip.cpu().numpy(), self.indices[pos].cpu().numpy(), *(v[pos].cpu().numpy() for v in values))
+
     def assemble(self, eps: torch.Tensor, mu_inv: torch.Tensor, E: torch.Tensor | None = None,
                  B: torch.Tensor | None = None):
         """Device call: eps, mu_inv complex128 (n_tets,) CUDA tensors -> (E, B) complex128 (nnz,)."""

@@ -127,6 +127,35 @@ def tet_mass_stiffness_matrices(field, er, ur):
     return E, B
 
 
+def rows_csr(field, er, ur, rows):
+    """Rows ``rows`` (ascending DOF ids) of the reference's E and B as CSR matrices of shape
+    (len(rows), N), without assembling the whole mesh.
+
+    Only the tets that touch one of the rows contribute to them; those tets run through
+    ``matrix_builder`` in ascending tet order, so every entry receives its contributions
+    in the same order as in the full COO array, and SciPy's ``tocsr`` sums them as the
+    reference's whole-mesh ``tocsr`` does (fem/physics/edm/optimized_assembly.py:61-62).
+    """
+    import types
+    from scipy.sparse import coo_matrix
+    m = field.mesh
+    rows = np.asarray(rows, dtype=np.int64)
+    N = 2 * m.edges.shape[1] + 2 * m.tris.shape[1]
+    t2f = np.asarray(field.tet_to_field, dtype=np.int64)
+    touch = np.isin(t2f, rows).any(axis=0)
+    sel = np.flatnonzero(touch)
+    sub_mesh = types.SimpleNamespace(nodes=m.nodes, tets=np.asarray(m.tets)[:, sel], tris=m.tris, edges=m.edges,
+                                     edge_lengths=m.edge_lengths, tet_to_edge=np.asarray(m.tet_to_edge)[:, sel])
+    sub = types.SimpleNamespace(mesh=sub_mesh, tet_to_field=t2f[:, sel])
+    dE, dB, r, c = matrix_builder(sub, np.asarray(er)[:, :, sel], np.asarray(ur)[:, :, sel])
+    local = np.searchsorted(rows, r)
+    keep = (local < len(rows)) & (rows[np.minimum(local, len(rows) - 1)] == r)
+    shape = (len(rows), N)
+    E = coo_matrix((dE[keep], (local[keep], c[keep])), shape=shape).tocsr()
+    B = coo_matrix((dB[keep], (local[keep], c[keep])), shape=shape).tocsr()
+    return E, B, len(sel)
+
+
 def tri_stiff_force(lcs_vertices, gamma, Uinc, DPTs):
     """ned2_tri_stiff_force (fem/mth/tri.py:575-695) -> (B 8x8, b 8)."""
     lv = _c(lcs_vertices, np.float64)
