@@ -89,6 +89,16 @@ class PortModes:
     solve_ids: np.ndarray
 
 
+@dataclass
+class PortProblem:
+    """The restricted 2-D port eigenproblem A x = lambda B x (dense, on the device)."""
+    A: torch.Tensor             # (n, n) complex128, PEC DOFs removed
+    B: torch.Tensor
+    solve_ids: np.ndarray       # kept DOFs of the surface numbering
+    surface: PortSurface
+    target_kz: float            # the reference's default search target (or the one given)
+
+
 def port_modes(field, er, ur, port_tags, basis, k0: float, pec_tags=(), target_kz: float | None = None,
                nmodes: int | None = None, face_block: bool = False,
                device: str | torch.device = "cuda") -> PortModes:
@@ -108,6 +118,33 @@ def port_modes(field, er, ur, port_tags, basis, k0: float, pec_tags=(), target_k
             TE10 constant of a WR-90 port 4.9 % above the analytic value at any
             mesh size; with the block integrated it converges to it.
     """
+    dev = torch.device(device)
+    pp = port_problem(field, er, ur, port_tags, basis, k0, pec_tags, target_kz, face_block, device)
+    As, Bs, S, solve_ids, target_kz = pp.A, pp.B, pp.surface, pp.solve_ids, pp.target_kz
+    N = S.n_field
+    sid = torch.as_tensor(solve_ids, device=dev)
+    sigma = -float(target_kz) ** 2
+    mu, vec = torch.linalg.eig(torch.linalg.solve(As - sigma * Bs, Bs))
+    mu = mu.cpu().numpy()
+    finite = np.abs(mu) > 1e-12 * np.abs(mu).max()
+    lam = np.full(mu.shape, np.inf + 0j)
+    lam[finite] = sigma + 1.0 / mu[finite]
+    lr = lam.real
+    keep = np.flatnonzero((lr <= -1) & (lr >= -(target_kz ** 2) * 8))
+    beta = np.sqrt(-lam[keep])
+    order = np.argsort(np.abs(beta - target_kz))
+    keep, beta = keep[order], beta[order]
+    if nmodes is not None:
+        keep, beta = keep[:nmodes], beta[:nmodes]
+    modes = torch.zeros((N, keep.size), dtype=torch.complex128, device=dev)
+    modes[sid] = vec[:, torch.as_tensor(keep, device=dev)]
+    return PortModes(beta, lam[keep], modes, S, solve_ids)
+
+
+def port_problem(field, er, ur, port_tags, basis, k0: float, pec_tags=(), target_kz: float | None = None,
+                 face_block: bool = False, device: str | torch.device = "cuda") -> PortProblem:
+    """Steps 1-4 of ``port_modes``: the PEC-restricted dense A and B of the port face (the
+    matrices the reference hands to ``SolveRoutine.eig``, emfreq3d.py:315)."""
     from .assembly import matinv_tensors
     dev = torch.device(device)
     m = field.mesh
@@ -169,19 +206,4 @@ def port_modes(field, er, ur, port_tags, basis, k0: float, pec_tags=(), target_k
         d = np.concatenate([er_t[0, 0], er_t[1, 1], er_t[2, 2]])
         u = np.concatenate([ur_t[0, 0], ur_t[1, 1], ur_t[2, 2]])
         target_kz = float(np.mean(d.real) * np.mean(u.real) * 0.65 * k0)
-    sigma = -float(target_kz) ** 2
-    mu, vec = torch.linalg.eig(torch.linalg.solve(As - sigma * Bs, Bs))
-    mu = mu.cpu().numpy()
-    finite = np.abs(mu) > 1e-12 * np.abs(mu).max()
-    lam = np.full(mu.shape, np.inf + 0j)
-    lam[finite] = sigma + 1.0 / mu[finite]
-    lr = lam.real
-    keep = np.flatnonzero((lr <= -1) & (lr >= -(target_kz ** 2) * 8))
-    beta = np.sqrt(-lam[keep])
-    order = np.argsort(np.abs(beta - target_kz))
-    keep, beta = keep[order], beta[order]
-    if nmodes is not None:
-        keep, beta = keep[:nmodes], beta[:nmodes]
-    modes = torch.zeros((N, keep.size), dtype=torch.complex128, device=dev)
-    modes[sid] = vec[:, torch.as_tensor(keep, device=dev)]
-    return PortModes(beta, lam[keep], modes, S, solve_ids)
+    return PortProblem(As, Bs, solve_ids, S, float(target_kz))

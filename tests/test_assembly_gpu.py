@@ -223,3 +223,31 @@ def test_cube80_row_blocks_match_oracle(torch_cuda):
     assert p["tets"] >= 10_000
     assert p["pattern_exact"]
     assert p["max_rel_E"] <= TOL and p["max_rel_B"] <= TOL, p
+
+
+@pytest.mark.parametrize("orient", ["descending", "mixed"])
+def test_edge_and_face_orientations(torch_cuda, orient):
+    """Edge and face orientations other than ascending vertex ids.  ``descending``: every
+    edge and face vertex list reversed, so each tet still follows one vertex order (the
+    canonical-frame fill); ``mixed``: a random half of the edges reversed, so some tets
+    follow no single order (the per-lane fill).  Both against the oracle, which evaluates
+    the reference's element formulas with whatever orientation the mesh arrays give."""
+    import types
+    from emerge_gb300.assembly import tet_mass_stiffness_matrices
+    from emerge_gb300.mesh import Nedelec2Basis, unit_cube
+    m = unit_cube(5, jitter=0.15, seed=4)
+    base = Nedelec2Basis(m)
+    edges, tris = np.array(m.edges), np.array(m.tris)
+    if orient == "descending":
+        edges, tris = edges[::-1].copy(), tris[::-1].copy()
+    else:
+        flip = np.random.default_rng(2).random(edges.shape[1]) < 0.5
+        edges[:, flip] = edges[::-1, flip]
+    mesh = types.SimpleNamespace(nodes=m.nodes, tets=m.tets, edges=edges, tris=tris, edge_lengths=m.edge_lengths,
+                                 tet_to_edge=m.tet_to_edge, tet_to_tri=m.tet_to_tri, tri_to_edge=m.tri_to_edge)
+    field = types.SimpleNamespace(mesh=mesh, tet_to_field=base.tet_to_field)
+    er, ur = _random_materials(m.n_tets, 8, mu_one=False)
+    E, B = tet_mass_stiffness_matrices(field, er, ur)
+    Eo, Bo = oracle.tet_mass_stiffness_matrices(field, er, ur)
+    assert rel_to_rowmax(E, Eo) <= TOL
+    assert rel_to_rowmax(B, Bo) <= TOL
