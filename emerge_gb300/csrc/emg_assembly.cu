@@ -783,7 +783,8 @@ extern "C" int emg_plan_create(int64_t n_nodes, int64_t n_tets, int64_t n_edges,
     TRY(check_err_flag(d_err, s));
     // fast fill: float-float blocks for entities within its limits
     TRY(df_plan_build(nodes, n_nodes, tets, n_tets, edges, n_edges, tris, n_tris, tet_to_field, tet_to_edge,
-                      edge_lengths, p->ent_list, p->n_ent, p->inc_ptr, p->inc, p->indptr, &p->df, s));
+                      edge_lengths, p->ent_list, p->n_ent, p->partner, p->inc_ptr, p->inc, 10 * n_tets, p->indptr,
+                      p->indices, &p->df, s));
     // FP64 records: the fill of entities outside the fast-fill limits and of tensor materials
     if (n_tets > 0) {
         TRY(dalloc(&p->recs, n_tets, "tet records"));

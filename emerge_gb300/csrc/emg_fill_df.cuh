@@ -11,9 +11,21 @@ constexpr int kDfMaxCols = 128;  // CSR columns per entity handled by the fast f
 
 // Device arrays of the fast fill, owned by the assembly plan.
 struct DfPlan {
-    void* recs = nullptr;        // per-tet normalised float-float invariants (448 B/tet)
+    void* recs = nullptr;        // per-tet normalised float-float invariants (448 B/tet; general meshes)
     double2* gscale = nullptr;   // per-tet FP64 scales of the curl-curl and mass blocks
     float4* tscale = nullptr;    // per-tet complex material scales (written by each fill)
+    // canonical-frame fill (every tet's orientations follow one vertex order): per-tet
+    // invariants (43 x nT float pairs), DOF ids in canonical slot order (nT x 20),
+    // incidences with canonical slots and their CSR positions, entity descriptors, and
+    // the staging buffer of the element blocks
+    bool canon = false;
+    float2* inv = nullptr;
+    int32_t* dofc = nullptr;
+    int64_t* inc_c = nullptr;
+    uint8_t* ipos = nullptr;     // CSR position of each incidence's 20 columns in its entity's row
+    void* edesc = nullptr;       // per fast-fill entity: CSR row offsets, first incidence, sizes
+    float4* st = nullptr;        // staged element blocks, (tet, row pair, column)-major: nT x 10 x 20 x 2 float4
+    int* mu_flag = nullptr;      // set by a fill whose mu^-1 has an imaginary part
     int2* groups = nullptr;      // warp work units: (first index into gents, entity count)
     int32_t* gents = nullptr;    // fast-fill entities ordered by class (2 edges / 1 edge / 6 faces per unit)
     int32_t* slow = nullptr;     // entities outside the fast-fill limits (FP64 fill)
@@ -23,8 +35,9 @@ struct DfPlan {
 
 int df_plan_build(const double* nodes, int64_t nN, const int32_t* tets, int64_t nT, const int32_t* edges, int64_t nE,
                   const int32_t* tris, int64_t nTri, const int32_t* t2f, const int32_t* t2e, const double* edge_len,
-                  const int32_t* ent_list, int64_t n_ent, const int64_t* inc_ptr, const int64_t* inc,
-                  const int64_t* indptr, DfPlan* p, cudaStream_t s);
+                  const int32_t* ent_list, int64_t n_ent, const int32_t* partner, const int64_t* inc_ptr,
+                  const int64_t* inc, int64_t n_inc, const int64_t* indptr, const int32_t* indices, DfPlan* p,
+                  cudaStream_t s);
 
 int df_fill(const DfPlan& p, int64_t nT, const int32_t* partner, const int64_t* inc_ptr, const int64_t* inc,
             const int64_t* indptr, const int32_t* indices, const double* eps, const double* mu_inv, double* E,
