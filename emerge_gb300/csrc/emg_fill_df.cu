@@ -740,12 +740,18 @@ __global__ void k_inc_pos(const int32_t* __restrict__ ent_list, int64_t n_ent, c
     }
 }
 
-// Staging layout (row-pair major): for tet t, entity slot s (the row pair) and column
-// c = j + 10 b (column slot j, mode b), two float4 at st + ((t * 10 + s) * 20 + c) * 2:
-// (D[0][c], D[1][c]) and (F[0][c], F[1][c]), float-float, rows 0 and 1 of the pair.  The
-// owner pass reads the 20 columns of a (tet, row pair) as one contiguous 640-byte run.
+// Staging layout: for tet t, entity slot s (the row pair) and column c = j + 10 b
+// (column slot j, mode b), one 32-byte unit of two float4: (D[0][c], D[1][c]) and
+// (F[0][c], F[1][c]), float-float, rows 0 and 1 of the pair.  Units are interleaved over
+// blocks of kStBlk consecutive tets, unit index ((t / kStBlk * 10 + s) * 20 + c) * kStBlk
+// + t % kStBlk: the element kernel's warp (one tet per lane) stores whole lines, and the
+// owner pass reads the 20 columns of a (tet, row pair) as 20 full sectors.
+constexpr int kStBlk = 8;
+__host__ __device__ __forceinline__ int64_t st_unit(int64_t t, int s, int c) {
+    return ((t / kStBlk * 10 + s) * 20 + c) * kStBlk + (t % kStBlk);
+}
 __device__ __forceinline__ void st_col(float4* st, int64_t t, int s, int c, df d0, df d1, df f0, df f1) {
-    float4* o = st + ((t * 10 + s) * 20 + c) * 2;
+    float4* o = st + st_unit(t, s, c) * 2;
     o[0] = make_float4(d0.h, d0.l, d1.h, d1.l);
     o[1] = make_float4(f0.h, f0.l, f1.h, f1.l);
 }
@@ -832,17 +838,27 @@ __global__ void k_ent_desc(const int32_t* __restrict__ gents, int64_t n, const i
     }
 }
 
-// Owner pass, warp per entity group.  The entities of a group are done one after another;
-// for each, its incident tets in ascending order: lane c < 20 takes column c (slot c % 10,
-// mode c / 10) of the tet's staged row pair, i.e. one CSR position of the entity's rows,
-// and adds the scaled D and F entries of both rows into the entity's accumulators in
-// shared memory.  A tet's 20 columns are 20 different positions, so the lanes never
-// collide, and every position sums its contributions in tet order (deterministic, bitwise
-// repeatable).  The next tet's run is loaded while the current one is added.
+// Owner pass, warp per entity group.  At the start of a group its entity descriptors and
+// incidences go to shared memory; the group's incident tets then run as one sequence,
+// entity after entity, each entity's tets in ascending order.  For each tet, lane c < 20
+// takes column c (slot c % 10, mode c / 10) of the tet's staged row pair, i.e. one CSR
+// position of the entity's rows, and adds the scaled D and F entries of both rows into
+// the entity's accumulators in shared memory.  A tet's 20 columns are 20 different
+// positions, so the lanes never collide, and every position sums its contributions in
+// tet order (deterministic, bitwise repeatable).  The next tet's run is loaded while the
+// current one is added, across entity boundaries too; an entity's rows are converted and
+// stored after its last tet.  The kernel runs in two modes: IM = false accumulates Re E,
+// Re B and Im B and writes E and B (Im E = 0); IM = true, launched after it, returns at
+// once unless some tet's mu^-1 is complex, and then accumulates Im E and writes it.
+constexpr int kAcc = 3;                 // accumulators per (row, position)
 struct __align__(16) OwnSm {
-    float2 acc[2 * kNmax * 4];          // [row][position][E re, E im, B re, B im] compensated (s, e)
+    float2 acc[2 * kNmax * kAcc];       // [row][position][component] compensated (s, e)
+    EntDesc ed[kGmax];
+    int64_t iidx[kKmax];                // incidence index of each step
     int32_t tet[kKmax];
     int8_t slot[kKmax];
+    int8_t ent[kKmax];                  // entity (within the group) of each step
+    int32_t kofs[kGmax + 1];
 };
 constexpr int kOwnWarps = 4;
 constexpr size_t kStSmem = sizeof(OwnSm) * kOwnWarps;
@@ -859,6 +875,7 @@ __device__ __forceinline__ void acc_sm(float2& c, df x, df y) {   // c += x * y
     c.x = t;
 }
 
+template <bool IM>
 __global__ void __launch_bounds__(32 * kOwnWarps) k_fill_st(const float4* __restrict__ st, const uint8_t* __restrict__ ipos,
                                                             const int2* __restrict__ groups, int64_t n_groups,
                                                             const EntDesc* __restrict__ edesc,
@@ -866,70 +883,100 @@ __global__ void __launch_bounds__(32 * kOwnWarps) k_fill_st(const float4* __rest
                                                             const float4* __restrict__ tscale,
                                                             const int* __restrict__ complex_mu,
                                                             double2* __restrict__ E, double2* __restrict__ B) {
+    if (IM && *complex_mu == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     OwnSm* sm_all = reinterpret_cast<OwnSm*>(smem_raw);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     OwnSm& sm = sm_all[w];
-    const bool e_real = *complex_mu == 0;
+    constexpr int nc = IM ? 1 : kAcc;
     for (int64_t g = blockIdx.x * (int64_t)kOwnWarps + w; g < n_groups; g += (int64_t)gridDim.x * kOwnWarps) {
         const int2 gr = groups[g];
-        for (int u = 0; u < gr.y; ++u) {
-            const EntDesc ed = edesc[gr.x + u];
-            const int n = ed.n, k = ed.k;
-            if (lane < k) {
-                const int64_t code = inc_c[ed.i0 + lane];
-                sm.tet[lane] = (int32_t)(code >> 4);
-                sm.slot[lane] = (int8_t)(code & 15);
+        const int nsub = gr.y;
+        if (lane < nsub) sm.ed[lane] = edesc[gr.x + lane];
+        __syncwarp();
+        if (lane == 0) {
+            int ko = 0;
+            for (int u = 0; u < nsub; ++u) {
+                sm.kofs[u] = ko;
+                ko += sm.ed[u].k;
             }
-            for (int i = lane; i < 2 * n * 4; i += 32) sm.acc[i] = make_float2(0.f, 0.f);
-            __syncwarp();
-            float4 cd = {}, cf = {}, cse = {}, csb = {}, nd = {}, nf = {}, nse = {}, nsb = {};
-            int cp = 0, np = 0;
+            sm.kofs[nsub] = ko;
+        }
+        __syncwarp();
+        const int ktot = sm.kofs[nsub];
+        int nmax = 0;
+        for (int u = 0; u < nsub; ++u) nmax = max(nmax, sm.ed[u].n);
+        if (lane < ktot) {
+            int u = 0;
+            while (lane >= sm.kofs[u + 1]) ++u;
+            const int64_t ii = sm.ed[u].i0 + (lane - sm.kofs[u]);
+            const int64_t code = inc_c[ii];
+            sm.iidx[lane] = ii;
+            sm.tet[lane] = (int32_t)(code >> 4);
+            sm.slot[lane] = (int8_t)(code & 15);
+            sm.ent[lane] = (int8_t)u;
+        }
+        for (int i = lane; i < 2 * nmax * nc; i += 32) sm.acc[i] = make_float2(0.f, 0.f);
+        __syncwarp();
+        float4 cd = {}, cf = {}, cse = {}, csb = {}, nd = {}, nf = {}, nse = {}, nsb = {};
+        int cp = 0, np = 0;
+        if (lane < 20) {
+            const int64_t t = sm.tet[0];
+            const float4* r = st + st_unit(t, sm.slot[0], lane) * 2;
+            cd = __ldg(r);
+            if (!IM) cf = __ldg(r + 1);
+            cse = __ldg(tscale + 2 * t);
+            if (!IM) csb = __ldg(tscale + 2 * t + 1);
+            cp = __ldg(ipos + sm.iidx[0] * 20 + lane);
+        }
+        for (int i = 0; i < ktot; ++i) {
+            const int u = sm.ent[i];
+            const int n = sm.ed[u].n;
             if (lane < 20) {
-                const int64_t t = sm.tet[0];
-                const float4* r = st + ((t * 10 + sm.slot[0]) * 20 + lane) * 2;
-                cd = __ldg(r);
-                cf = __ldg(r + 1);
-                cse = __ldg(tscale + 2 * t);
-                csb = __ldg(tscale + 2 * t + 1);
-                cp = __ldg(ipos + ed.i0 * 20 + lane);
-            }
-            for (int q = 0; q < k; ++q) {
-                if (lane < 20) {
-                    if (q + 1 < k) {
-                        const int64_t t = sm.tet[q + 1];
-                        const float4* r = st + ((t * 10 + sm.slot[q + 1]) * 20 + lane) * 2;
-                        nd = __ldg(r);
-                        nf = __ldg(r + 1);
-                        nse = __ldg(tscale + 2 * t);
-                        nsb = __ldg(tscale + 2 * t + 1);
-                        np = __ldg(ipos + (ed.i0 + q + 1) * 20 + lane);
-                    }
-                    float2* c0 = sm.acc + cp * 4;
-                    float2* c1 = sm.acc + (n + cp) * 4;
-                    const df D0 = mk(cd.x, cd.y), D1 = mk(cd.z, cd.w), F0 = mk(cf.x, cf.y), F1 = mk(cf.z, cf.w);
+                if (i + 1 < ktot) {
+                    const int64_t t = sm.tet[i + 1];
+                    const float4* r = st + st_unit(t, sm.slot[i + 1], lane) * 2;
+                    nd = __ldg(r);
+                    if (!IM) nf = __ldg(r + 1);
+                    nse = __ldg(tscale + 2 * t);
+                    if (!IM) nsb = __ldg(tscale + 2 * t + 1);
+                    np = __ldg(ipos + sm.iidx[i + 1] * 20 + lane);
+                }
+                float2* c0 = sm.acc + cp * nc;
+                float2* c1 = sm.acc + (n + cp) * nc;
+                const df D0 = mk(cd.x, cd.y), D1 = mk(cd.z, cd.w);
+                if (IM) {
+                    acc_sm(c0[0], mk(cse.z, cse.w), D0);
+                    acc_sm(c1[0], mk(cse.z, cse.w), D1);
+                } else {
+                    const df F0 = mk(cf.x, cf.y), F1 = mk(cf.z, cf.w);
                     acc_sm(c0[0], mk(cse.x, cse.y), D0);
                     acc_sm(c1[0], mk(cse.x, cse.y), D1);
-                    if (!e_real) {
-                        acc_sm(c0[1], mk(cse.z, cse.w), D0);
-                        acc_sm(c1[1], mk(cse.z, cse.w), D1);
-                    }
-                    acc_sm(c0[2], mk(csb.x, csb.y), F0);
-                    acc_sm(c1[2], mk(csb.x, csb.y), F1);
-                    acc_sm(c0[3], mk(csb.z, csb.w), F0);
-                    acc_sm(c1[3], mk(csb.z, csb.w), F1);
+                    acc_sm(c0[1], mk(csb.x, csb.y), F0);
+                    acc_sm(c1[1], mk(csb.x, csb.y), F1);
+                    acc_sm(c0[2], mk(csb.z, csb.w), F0);
+                    acc_sm(c1[2], mk(csb.z, csb.w), F1);
                 }
-                __syncwarp();
-                cd = nd; cf = nf; cse = nse; csb = nsb; cp = np;
-            }
-            for (int i = lane; i < 2 * n; i += 32) {
-                const int a = i >= n ? 1 : 0, p = i - a * n;
-                const float2* c = sm.acc + (a * n + p) * 4;
-                const int64_t o = (a == 0 ? ed.b1 : ed.b2) + p;
-                E[o] = make_double2(to_double(fts(c[0].x, c[0].y)), e_real ? 0.0 : to_double(fts(c[1].x, c[1].y)));
-                B[o] = make_double2(to_double(fts(c[2].x, c[2].y)), to_double(fts(c[3].x, c[3].y)));
             }
             __syncwarp();
+            cd = nd; cf = nf; cse = nse; csb = nsb; cp = np;
+            if (i + 1 == ktot || sm.ent[i + 1] != u) {
+                const EntDesc& ed = sm.ed[u];
+                for (int x = lane; x < 2 * n; x += 32) {
+                    const int a = x >= n ? 1 : 0, p = x - a * n;
+                    float2* c = sm.acc + (a * n + p) * nc;
+                    const int64_t o = (a == 0 ? ed.b1 : ed.b2) + p;
+                    if (IM) {
+                        reinterpret_cast<double*>(E + o)[1] = to_double(fts(c[0].x, c[0].y));
+                    } else {
+                        E[o] = make_double2(to_double(fts(c[0].x, c[0].y)), 0.0);
+                        B[o] = make_double2(to_double(fts(c[1].x, c[1].y)), to_double(fts(c[2].x, c[2].y)));
+                    }
+#pragma unroll
+                    for (int cc = 0; cc < nc; ++cc) c[cc] = make_float2(0.f, 0.f);
+                }
+                __syncwarp();
+            }
         }
     }
 }
@@ -1074,7 +1121,8 @@ int df_plan_build(const double* nodes, int64_t nN, const int32_t* tets, int64_t 
                                                                             indptr, indices, p->ipos);
             TRYC(cudaGetLastError());
         }
-        TRY(dalloc(&p->st, (int64_t)nT * 10 * 20 * 2, "df staged element blocks"));
+        TRY(dalloc(&p->st, (nT + dfk::kStBlk - 1) / dfk::kStBlk * dfk::kStBlk * 10 * 20 * 2,
+                   "df staged element blocks"));
         TRY(dalloc(&p->mu_flag, 1, "df complex-mu flag"));
     } else {
         dfree(p->inv);
@@ -1141,7 +1189,9 @@ int df_fill(const DfPlan& p, int64_t nT, const int32_t* partner, const int64_t* 
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
         EMG_CUDA(cudaFuncSetAttribute(dfk::k_fill_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)dfk::kFillSmem));
-        EMG_CUDA(cudaFuncSetAttribute(dfk::k_fill_st, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        EMG_CUDA(cudaFuncSetAttribute(dfk::k_fill_st<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)dfk::kStSmem));
+        EMG_CUDA(cudaFuncSetAttribute(dfk::k_fill_st<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)dfk::kStSmem));
         attr_set[dev] = true;
     }
@@ -1156,7 +1206,12 @@ int df_fill(const DfPlan& p, int64_t nT, const int32_t* partner, const int64_t* 
         dfk::k_elem<<<grid_for(nT, dfk::kElemThreads, 152u * 64u), dfk::kElemThreads, 0, s>>>(p.inv, nT, p.st);
         EMG_CUDA(cudaGetLastError());
         const unsigned g = grid_for(p.n_groups, dfk::kOwnWarps, 152u * 16u);
-        dfk::k_fill_st<<<g, 32 * dfk::kOwnWarps, dfk::kStSmem, s>>>(
+        dfk::k_fill_st<false><<<g, 32 * dfk::kOwnWarps, dfk::kStSmem, s>>>(
+            p.st, p.ipos, reinterpret_cast<const int2*>(p.groups), p.n_groups,
+            reinterpret_cast<const dfk::EntDesc*>(p.edesc), p.inc_c, p.tscale, p.mu_flag,
+            reinterpret_cast<double2*>(E), reinterpret_cast<double2*>(B));
+        EMG_CUDA(cudaGetLastError());
+        dfk::k_fill_st<true><<<g, 32 * dfk::kOwnWarps, dfk::kStSmem, s>>>(
             p.st, p.ipos, reinterpret_cast<const int2*>(p.groups), p.n_groups,
             reinterpret_cast<const dfk::EntDesc*>(p.edesc), p.inc_c, p.tscale, p.mu_flag,
             reinterpret_cast<double2*>(E), reinterpret_cast<double2*>(B));

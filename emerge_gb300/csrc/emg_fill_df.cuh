@@ -24,7 +24,7 @@ struct DfPlan {
     int64_t* inc_c = nullptr;
     uint8_t* ipos = nullptr;     // CSR position of each incidence's 20 columns in its entity's row
     void* edesc = nullptr;       // per fast-fill entity: CSR row offsets, first incidence, sizes
-    float4* st = nullptr;        // staged element blocks, (tet, row pair, column)-major: nT x 10 x 20 x 2 float4
+    float4* st = nullptr;        // staged element blocks: 32 B per (tet, row pair, column), tets interleaved by 8
     int* mu_flag = nullptr;      // set by a fill whose mu^-1 has an imaginary part
     int2* groups = nullptr;      // warp work units: (first index into gents, entity count)
     int32_t* gents = nullptr;    // fast-fill entities ordered by class (2 edges / 1 edge / 6 faces per unit)
