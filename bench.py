@@ -121,6 +121,13 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def issue_floor_ms(warp_inst: float, clocks: dict) -> float:
+    """Time to issue ``warp_inst`` warp instructions on 152 SMs x 4 schedulers at the SM
+    clock sampled during the timed region (its maximum when no sample was taken)."""
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    return warp_inst / (152 * 4 * mhz * 1e6) * 1e3
+
+
 def traffic_per_launch(n: int):
     """DRAM bytes per fill launch from the committed ncu summary (scaled by tets), or None."""
     p = os.path.join(ROOT, "profiles", "assembly_fill_traffic.json")
@@ -178,8 +185,10 @@ def run_reference(args, rank, world):
 
 # FP64 flops per tet of the factored isotropic element blocks plus the complex
 # material scaling and accumulation (36 ee x 40 + 48 ef/fe x 73 + 16 ff x 129 + 100 x 36)
-FILL_FLOPS_PER_TET = 10608
-FP64_TFLOPS = 1.18      # GB300 DFMA throughput measured by a probe kernel
+# warp instructions per tet of one fill (k_elem 1274 + k_fill_st 3570), from the ncu
+# capture summarised in profiles/k_elem_k_fill_st_cube40.md; the fill runs on the FP32 and
+# integer pipes, so its compute bound is the issue rate of 152 SMs x 4 schedulers
+FILL_WARP_INST_PER_TET = 4844
 
 
 def run_gpu(args, rank, world):
@@ -284,14 +293,16 @@ def run_gpu(args, rank, world):
                        "what": "new plan (pattern + records) + fill + D2H of values and pattern, one call"},
         "parity": parity,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "kernel": "k_scales + k_fill_df (one assembly step)",
+                     "peak_source": peak_kind,
+                     "kernel": "one assembly step: k_scales + k_elem + k_fill_st (+ its Im E pass, empty for real mu)",
                      "algorithmic_bytes_per_launch": int(alg_bytes), "traffic": traffic_per_launch(n),
-                     # the element arithmetic: FP64 flops of the factored isotropic block formulas
-                     # per tet (counted from the FP64 fill's formulas) at GB300's measured DFMA rate
-                     "compute": {"bound": "fp64-equivalent", "flops_per_tet": FILL_FLOPS_PER_TET,
-                                 "peak_tflops": FP64_TFLOPS, "floor_ms": FILL_FLOPS_PER_TET * nT / FP64_TFLOPS / 1e9,
-                                 "frac": FILL_FLOPS_PER_TET * nT / FP64_TFLOPS / 1e9 / statistics.median(launch_ms)}},
-        "gpu_launches": 2 * args.steps,
+                     # the float-float arithmetic runs on the FP32/integer pipes: its bound is the
+                     # warp-instruction issue rate at the sampled SM clock
+                     "compute": {"bound": "issue (FP32 float-float)", "warp_inst_per_tet": FILL_WARP_INST_PER_TET,
+                                 "floor_ms": issue_floor_ms(FILL_WARP_INST_PER_TET * nT, clk.summary()),
+                                 "frac": issue_floor_ms(FILL_WARP_INST_PER_TET * nT, clk.summary())
+                                 / statistics.median(launch_ms)}},
+        "gpu_launches": 4 * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0:
