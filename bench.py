@@ -185,6 +185,8 @@ def run_reference(args, rank, world):
 
 # FP64 flops per tet of the factored isotropic element blocks plus the complex
 # material scaling and accumulation (36 ee x 40 + 48 ef/fe x 73 + 16 ff x 129 + 100 x 36)
+FP64_TFLOPS = 1.18         # GB300 FP64 FMA throughput measured by a probe kernel (DFMA chain)
+FP32_TFLOPS = 74.8         # GB300 FP32 FMA throughput measured by a probe kernel
 # warp instructions per tet of one fill (k_elem 1274 + k_fill_st 3570), from the ncu
 # capture summarised in profiles/k_elem_k_fill_st_cube40.md; the fill runs on the FP32 and
 # integer pipes, so its compute bound is the issue rate of 152 SMs x 4 schedulers
@@ -379,6 +381,80 @@ def run_topology(m, n, dev):
             "identical_to_host": bool(same)}
 
 
+def _median_event_ms(fn, reps: int = 5, warm: int = 2) -> float:
+    """Median CUDA-event time (ms) of fn() on the current stream."""
+    import torch
+    for _ in range(warm):
+        fn()
+    st = torch.cuda.current_stream()
+    ts = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(st)
+        fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    return statistics.median(ts)
+
+
+def sweep_rooflines(sw, freqs, n_anchor: int, chunk: int) -> dict:
+    """HBM rooflines of the sweep's two memory-bound operators, timed alone with CUDA events
+    on one chunk of the sweep's columns (c frequencies x 2 ports):
+
+      spmv       — ``emg_spmv`` (kernel k_spmv / k_spmv_w): Y = A(k_c) X for every column,
+                   A stored [nnz_r][c] complex128.  Algorithmic bytes per launch:
+                   16 nnz_r c (matrix values, each read once) + 4 nnz_r (column indices)
+                   + 8 (n+1) (row pointers) + 2 x 16 n 2c (X read, Y written).
+      slab_apply — ``emg_slab_apply``: every column through its anchor's complex-FP32 slab
+                   factor (forward and backward block sweep).  Algorithmic bytes: each used
+                   factor's dense slab inverses read twice (2 x 8 sum w_i^2 per factor) +
+                   4 x 16 n 2c (the right-hand side read, the result written, the forward
+                   sweep's intermediate written and read back).
+    """
+    import torch
+    peak, kind = peaks()
+    c = max(1, min(len(freqs), chunk))
+    fr = np.asarray(freqs[:c], dtype=float)
+    k0, gam, _ = sw._coeffs(fr)
+    A = sw.sys.form(sw.E, sw.B, k0 ** 2, sw.P, gam)
+    n, nnz = sw.sys.n, sw.sys.nnz
+    npo = len(sw.ports)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    X = torch.randn((n, c * npo), dtype=torch.complex128, device="cuda", generator=gen)
+    cm = torch.arange(c, dtype=torch.int32, device="cuda").repeat_interleave(npo)
+    ms = _median_event_ms(lambda: sw.sys.spmv(A, X, cm))
+    b_spmv = 16 * nnz * c + 4 * nnz + 8 * (n + 1) + 2 * 16 * n * c * npo
+    anchors = sw.default_anchors(freqs, n_anchor)
+    sw.factor_anchors(anchors, "fp32")
+    near = np.argmin(np.abs(fr[:, None] - anchors[None, :]), axis=1)
+    cfac = np.repeat(near, npo)
+    sl = sw.slab()
+    off, _ = sl.levels()
+    w = np.diff(off)
+    ms_a = _median_event_ms(lambda: sl.apply(X, cfac))
+    b_apply = 2 * 8 * int(np.sum(w * w)) * len(np.unique(near)) + 4 * 16 * n * c * npo
+    del A, X
+    torch.cuda.empty_cache()
+    cols = c * npo
+    f_spmv = 8 * nnz * cols                          # complex FP64 multiply-add = 8 flops
+    f_apply = 2 * 8 * int(np.sum(w * w)) * cols      # two sweeps of complex FP32 multiply-adds
+    sp = {"ms": round(ms, 4), "algorithmic_bytes": int(b_spmv), "achieved": b_spmv / ms / 1e6, "peak": peak,
+          "unit": "GB/s", "frac": b_spmv / ms / 1e6 / peak,
+          "compute": {"pipe": "fp64", "flops": int(f_spmv), "achieved_tflops": f_spmv / ms / 1e9,
+                      "peak_tflops": FP64_TFLOPS, "frac": f_spmv / ms / 1e9 / FP64_TFLOPS}}
+    ap = {"ms": round(ms_a, 4), "algorithmic_bytes": int(b_apply), "achieved": b_apply / ms_a / 1e6, "peak": peak,
+          "unit": "GB/s", "frac": b_apply / ms_a / 1e6 / peak,
+          "compute": {"pipe": "fp32", "flops": int(f_apply), "achieved_tflops": f_apply / ms_a / 1e9,
+                      "peak_tflops": FP32_TFLOPS, "frac": f_apply / ms_a / 1e9 / FP32_TFLOPS},
+          "factors_used": int(len(np.unique(near))), "sum_w2": int(np.sum(w * w)), "slabs": int(len(w))}
+    for d in (sp, ap):
+        d["bound"] = "compute (" + d["compute"]["pipe"] + ")" if d["compute"]["frac"] > d["frac"] else "hbm"
+    return {"columns": int(cols), "matrices": int(c), "n": int(n), "nnz_r": int(nnz), "peak_source": kind,
+            "spmv": sp, "slab_apply": ap}
+
+
 def run_sweep(args):
     """Iris-filter sweep: batched + mixed-precision + warm-started vs the plain FP64 GPU solve.
 
@@ -395,7 +471,10 @@ def run_sweep(args):
       mlp    — the same with the BF16 tensor-core MLP (trained on ``--sweep-mlp-train``
                points) supplying the initial guesses instead of the projection.
       cold   — the same anchored batched FGMRES from zero initial guesses.
-    max|dS| compares each with plain on the plain points.  Also reported: the
+    max|dS| compares each with plain on the plain points (spread points plus the two
+    strongest passband peaks), and with an independent per-point check on 16 points
+    that include the five passband peaks (``check``).  ``roofline``: the HBM rooflines
+    of the SpMV and of the slab-factor apply (see sweep_rooflines).  Also reported: the
     ILU(0)-GMRES plain method on one point with capped iterations, and SciPy's
     SuperLU (the reference's default direct solver) per point on the host cores.
     """
@@ -425,6 +504,9 @@ def run_sweep(args):
     # the slab products' layout, tuned once per mesh and column pattern (not timed)
     out["autotune"] = sw.autotune(freqs, n_anchor=args.sweep_anchors, chunk=chunk)
     out["autotune"]["seconds"] = round(out["autotune"]["seconds"], 2)
+    out["roofline"] = sweep_rooflines(sw, freqs, args.sweep_anchors, chunk)
+    if args.sweep_rooflines_only:
+        return out
     kw = dict(precision="fp32", tol=args.sweep_tol, restart=args.sweep_restart, chunk=chunk,
               refine=args.sweep_refine, inner=args.sweep_inner)
     with ClockSampler(0) as clk:
@@ -442,13 +524,41 @@ def run_sweep(args):
                           n_anchor=args.sweep_anchors, guess="mlp", mlp_steps=args.sweep_mlp_steps, **kw)
         sw._slab_key = None
         cold = sw.run_anchored(freqs, n_anchor=args.sweep_anchors, **kw)
+        # the passband peaks of |S21| (resonances, where the sweep is hardest): the largest
+        # local maxima of the fast sweep's |S21|
+        s21 = np.abs(fast.S[:, 1, 0])
+        loc = np.flatnonzero((s21[1:-1] > s21[:-2]) & (s21[1:-1] >= s21[2:])) + 1
+        peaks_i = np.sort(loc[np.argsort(s21[loc])[::-1][:5]])
+        # the plain FP64 solver on spread points plus the two strongest peaks
+        idx = np.unique(np.concatenate([idx, peaks_i[np.argsort(s21[peaks_i])[::-1][:args.sweep_plain_peaks]]]))
         plain = sw.run(freqs[idx], method="plain", precond="slab64", tol=args.sweep_tol)
+    # independent check on 16 points (the peaks + spread points): every column
+    # preconditioned by a factorization at its own frequency, FGMRES to a 1e-12 FP64
+    # residual (no warm start, no shared anchors), untimed
+    spread = np.linspace(0, nf - 1, max(2, args.sweep_check - len(peaks_i)) + 2).astype(int)[1:-1]
+    chk = np.unique(np.concatenate([peaks_i, spread]))
+    sw._slab_key = None
+    check = sw.run_anchored(freqs[chk], anchors=freqs[chk], precision="fp32", tol=1e-12,
+                            restart=args.sweep_restart)
+    sw._slab_key = None
     v_fast = nf / fast.seconds
     v_plain = len(idx) / plain.seconds
     pred = mlp.info["final_index"]
+    common = np.flatnonzero(np.isin(chk, idx))
     out.update({
         "fast": v_fast, "plain": v_plain, "ratio": v_fast / v_plain,
         "max_abs_dS_vs_plain": float(np.max(np.abs(fast.S[idx] - plain.S))),
+        "plain_points_GHz": [round(float(f) / 1e9, 4) for f in freqs[idx]],
+        "check": {"points": int(len(chk)), "points_GHz": [round(float(f) / 1e9, 4) for f in freqs[chk]],
+                  "passband_peaks_GHz": [round(float(f) / 1e9, 4) for f in freqs[peaks_i]],
+                  "S21_dB_at_peaks": [round(float(20 * np.log10(s21[i] + 1e-300)), 3) for i in peaks_i],
+                  "method": "per point: complex-FP32 slab factor of A(k) at that frequency, FP64 FGMRES to 1e-12",
+                  "max_residual": float(check.residuals.max()),
+                  "max_abs_dS_fast": float(np.max(np.abs(fast.S[chk] - check.S))),
+                  "max_abs_dS_mlp": float(np.max(np.abs(mlp.S[chk] - check.S))),
+                  "max_abs_dS_cold": float(np.max(np.abs(cold.S[chk] - check.S))),
+                  "max_abs_dS_plain_vs_check": float(np.max(np.abs(plain.S[np.searchsorted(idx, chk[common])]
+                                                                   - check.S[common]))) if common.size else None},
         "max_residual_fast": float(fast.residuals.max()), "max_residual_plain": float(plain.residuals.max()),
         "fast_seconds": round(fast.seconds, 3), "plain_seconds_per_point": round(plain.seconds / len(idx), 3),
         "plain_points_timed": int(len(idx)), "anchors": args.sweep_anchors, "precision_inner": "complex fp32",
@@ -489,9 +599,6 @@ def run_sweep(args):
 # separately, sincosf excluded): phase 5, r x (n x H) 18, n x E - Z0 (...) 12,
 # rotation by G 18, accumulation of r x ie 24
 FF_FLOPS_PER_PAIR = 77
-FP32_TFLOPS = 74.8         # GB300 FP32 FMA throughput measured by a probe kernel
-
-
 def run_farfield(dev):
     """Stratton-Chu far field: 20k surface sources x 181 x 360 directions on the GPU,
     against the NumPy restatement on a 300-direction sample of the same sources."""
@@ -665,7 +772,11 @@ def main():
     ap.add_argument("--sweep-inner", default="fp64", choices=["fp32", "fp64"],
                     help="precision of the Krylov vectors of the fast sweep (its factors are FP32 either way)")
     ap.add_argument("--sweep-refine", type=int, default=0, help="Newton-Schulz step on the FP32 slab inverses")
-    ap.add_argument("--sweep-plain", type=int, default=2)
+    ap.add_argument("--sweep-plain", type=int, default=2, help="spread points timed with the plain FP64 solver")
+    ap.add_argument("--sweep-plain-peaks", type=int, default=2, help="passband peaks added to the plain points")
+    ap.add_argument("--sweep-check", type=int, default=16, help="points of the independent S-parameter check")
+    ap.add_argument("--sweep-rooflines-only", action="store_true",
+                    help="with --sweep-only: build the iris sweep and measure only the SpMV / slab-apply rooflines")
     ap.add_argument("--sweep-ilu-iters", type=int, default=1000)
     ap.add_argument("--sweep-cpu", type=int, default=1, help="points solved by SciPy SuperLU on the host")
     ap.add_argument("--sweep-tol", type=float, default=1e-8)

@@ -699,9 +699,9 @@ class FrequencySweep:
             X[:, f0 * npo:f1 * npo] = x
             its[f0 * npo:f1 * npo] = it
             res[f0 * npo:f1 * npo] = rs
-        torch.cuda.synchronize()
-        secs = time.perf_counter() - t0
+        # S-parameter extraction is part of the solve phase (it ends with a device-to-host copy)
         S = self._sparams(X, nf, beta, k0)
+        secs = time.perf_counter() - t0
         info = {"anchors": anchors, "precision": precision, "refine": refine, "inner": inner,
                 "refinement_steps": steps, "factor_seconds": t_fac, **sl.info()}
         return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X, info)
@@ -752,9 +752,8 @@ class FrequencySweep:
                 X[:, f0 * npo:f1 * npo] = x
                 its[f0 * npo:f1 * npo] = it
                 res[f0 * npo:f1 * npo] = rs
-        torch.cuda.synchronize()
-        secs = time.perf_counter() - t0
         S = self._sparams(X, nf, beta, k0)
+        secs = time.perf_counter() - t0
         return SweepResult(freqs, S, its.reshape(nf, npo), res.reshape(nf, npo), secs, X)
 
 
@@ -897,12 +896,16 @@ class FrequencySweep:
         # the training points are done: solve the others and keep their solutions
         others = np.setdiff1d(np.arange(nf), tr)
         x0_others = None if X0 is None else X0.reshape(-1, nf, npo)[:, others].reshape(X0.shape[0], -1)
-        rest_part = solve(freqs[others], x0_others)
+        if others.size:
+            rest_part = solve(freqs[others], x0_others)
+            rest = self._merge(freqs, tr, first, others, rest_part)
+            final_s = rest_part.seconds
+        else:                      # every point was a training point
+            rest_part, rest, final_s = first, first, 0.0
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
-        rest = self._merge(freqs, tr, first, others, rest_part)
         info = {"train_points": len(tr), "train_index": tr, "train_iterations": first.iterations,
-                "train_seconds": first.seconds, "guess_seconds": t_guess, "final_seconds": rest_part.seconds,
+                "train_seconds": first.seconds, "guess_seconds": t_guess, "final_seconds": final_s,
                 "final_index": others, "final_iterations_mean": float(rest_part.iterations.mean()) if others.size else 0.0,
                 "guess": guess, "mlp_loss": mlp_loss, "solver": solver,
                 **({k: v for k, v in first.info.items()} if solver == "anchored" else {})}
