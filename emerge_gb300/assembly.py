@@ -61,6 +61,20 @@ def scalar_material(m: np.ndarray, name: str) -> np.ndarray:
     return m[0, 0, :].astype(np.complex128)
 
 
+def matinv_device(s: torch.Tensor) -> torch.Tensor:
+    """matinv (fem/mth/optimized.py:440-461) on the GPU (``emg_matinv``): ``s`` complex128
+    CUDA tensor (9, n_tets) (the reference's (3,3,n) in C order) or (n_tets,) scalars
+    (isotropic tensors s*I, whose matinv is 1/s)."""
+    s = s.contiguous()
+    assert s.dtype == torch.complex128 and s.is_cuda
+    ncomp = 9 if s.dim() == 2 else 1
+    n = int(s.shape[-1])
+    out = torch.empty_like(s)
+    with torch.cuda.device(s.device):
+        _lib.call("emg_matinv", n, ncomp, _dptr(s), _dptr(out), _stream())
+    return out
+
+
 def matinv_tensors(s: np.ndarray) -> np.ndarray:
     """matinv (fem/mth/optimized.py:441-461) of every (3,3) slice of a (3,3,nT) array.
 
@@ -225,13 +239,14 @@ class AssemblyPlan:
         er = _check_tensor(er, "er")
         ur = _check_tensor(ur, "ur")
         if is_scalar_material(er) and is_scalar_material(ur):
-            eps, mu_inv = material_scalars(er, ur)
+            eps = scalar_material(er, "er")
+            mu = scalar_material(ur, "ur")
             return self.assemble(torch.as_tensor(eps, device=self.device),
-                                 torch.as_tensor(mu_inv, device=self.device))
+                                 matinv_device(torch.as_tensor(mu, device=self.device)))
         eps9 = np.ascontiguousarray(er, dtype=np.complex128).reshape(9, -1)
-        mu9 = np.ascontiguousarray(matinv_tensors(ur)).reshape(9, -1)
+        ur9 = np.ascontiguousarray(ur, dtype=np.complex128).reshape(9, -1)
         return self.assemble_tensor(torch.as_tensor(eps9, device=self.device),
-                                    torch.as_tensor(mu9, device=self.device))
+                                    matinv_device(torch.as_tensor(ur9, device=self.device)))
 
     def assemble_host(self, eps: np.ndarray, mu_inv: np.ndarray, E: np.ndarray | None = None,
                       B: np.ndarray | None = None):
@@ -275,11 +290,14 @@ def tet_mass_stiffness_matrices(field, er: np.ndarray, ur: np.ndarray):
     er = _check_tensor(er, "er")
     ur = _check_tensor(ur, "ur")
     if is_scalar_material(er) and is_scalar_material(ur):
-        eps, mu_inv = material_scalars(er, ur)
+        eps = scalar_material(er, "er")
+        mu = torch.as_tensor(scalar_material(ur, "ur"), device=plan.device)
+        mu_inv = matinv_device(mu).cpu().numpy()
         Ed, Bd = plan.assemble_host(eps, mu_inv)
     else:
+        ur9 = torch.as_tensor(np.ascontiguousarray(ur, dtype=np.complex128).reshape(9, -1), device=plan.device)
         Ed, Bd = plan.assemble_tensor_host(np.ascontiguousarray(er, dtype=np.complex128).reshape(9, -1),
-                                           matinv_tensors(ur).reshape(9, -1))
+                                           matinv_device(ur9).cpu().numpy())
     ip, ix = plan.pattern_host()
     N = plan.n_field
     E = csr_matrix((Ed, ix, ip), shape=(N, N))

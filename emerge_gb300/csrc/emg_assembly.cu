@@ -1071,3 +1071,78 @@ extern "C" int emg_csr_pattern_noalloc(int64_t n_tets, int64_t n_field, const in
     }
     return check_err_flag(d_err, s);
 }
+
+// ------------------------------------------------------------ materials ---
+namespace emg {
+namespace {
+__device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 csub2(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cadd2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 crecip(double2 z) {
+    const double d = z.x * z.x + z.y * z.y;
+    return make_double2(z.x / d, -z.y / d);
+}
+
+// matinv (fem/mth/optimized.py:440-461) per tet, thread per tet: a tensor whose six
+// off-diagonal entries are all zero gets its reciprocal diagonal; any other gets the
+// reference's adj(s) * det(s) (it multiplies by the determinant instead of dividing).
+// ncomp 9: s, out are complex (9, n) = the reference's (3,3,n) C order; ncomp 1: complex
+// scalars (isotropic tensors s * I), out = 1 / s.
+__global__ void k_matinv(int64_t n, int ncomp, const double2* __restrict__ s9, double2* __restrict__ o9) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        if (ncomp == 1) {
+            o9[t] = crecip(s9[t]);
+            continue;
+        }
+        double2 a[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) a[i][j] = s9[(i * 3 + j) * n + t];
+        bool diag = true;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                if (i != j && (a[i][j].x != 0.0 || a[i][j].y != 0.0)) diag = false;
+        double2 o[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) o[i][j] = make_double2(0.0, 0.0);
+        if (diag) {
+            for (int i = 0; i < 3; ++i) o[i][i] = crecip(a[i][i]);
+        } else {
+            // det and adjugate in the reference's term order
+            double2 det = cmul2(cmul2(a[0][0], a[1][1]), a[2][2]);
+            det = csub2(det, cmul2(cmul2(a[0][0], a[1][2]), a[2][1]));
+            det = csub2(det, cmul2(cmul2(a[0][1], a[1][0]), a[2][2]));
+            det = cadd2(det, cmul2(cmul2(a[0][1], a[1][2]), a[2][0]));
+            det = cadd2(det, cmul2(cmul2(a[0][2], a[1][0]), a[2][1]));
+            det = csub2(det, cmul2(cmul2(a[0][2], a[1][1]), a[2][0]));
+            const double2 neg = make_double2(-1.0, 0.0);
+            o[0][0] = csub2(cmul2(a[1][1], a[2][2]), cmul2(a[1][2], a[2][1]));
+            o[0][1] = cadd2(cmul2(cmul2(neg, a[0][1]), a[2][2]), cmul2(a[0][2], a[2][1]));
+            o[0][2] = csub2(cmul2(a[0][1], a[1][2]), cmul2(a[0][2], a[1][1]));
+            o[1][0] = cadd2(cmul2(cmul2(neg, a[1][0]), a[2][2]), cmul2(a[1][2], a[2][0]));
+            o[1][1] = csub2(cmul2(a[0][0], a[2][2]), cmul2(a[0][2], a[2][0]));
+            o[1][2] = cadd2(cmul2(cmul2(neg, a[0][0]), a[1][2]), cmul2(a[0][2], a[1][0]));
+            o[2][0] = csub2(cmul2(a[1][0], a[2][1]), cmul2(a[1][1], a[2][0]));
+            o[2][1] = cadd2(cmul2(cmul2(neg, a[0][0]), a[2][1]), cmul2(a[0][1], a[2][0]));
+            o[2][2] = csub2(cmul2(a[0][0], a[1][1]), cmul2(a[0][1], a[1][0]));
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) o[i][j] = cmul2(o[i][j], det);
+        }
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) o9[(i * 3 + j) * n + t] = o[i][j];
+    }
+}
+}  // namespace
+}  // namespace emg
+
+extern "C" int emg_matinv(int64_t n_tets, int ncomp, const double* s, double* out, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(n_tets >= 0 && (ncomp == 1 || ncomp == 9), "emg_matinv: bad size or ncomp (1 or 9)");
+    if (n_tets == 0) return EMG_OK;
+    EMG_CHECK_ARG(s != nullptr && out != nullptr, "emg_matinv: NULL array");
+    k_matinv<<<grid_for(n_tets, 256), 256, 0, (cudaStream_t)stream>>>(n_tets, ncomp, reinterpret_cast<const double2*>(s),
+                                                                      reinterpret_cast<double2*>(out));
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}

@@ -145,7 +145,7 @@ def port_problem(field, er, ur, port_tags, basis, k0: float, pec_tags=(), target
                  face_block: bool = False, device: str | torch.device = "cuda") -> PortProblem:
     """Steps 1-4 of ``port_modes``: the PEC-restricted dense A and B of the port face (the
     matrices the reference hands to ``SolveRoutine.eig``, emfreq3d.py:315)."""
-    from .assembly import matinv_tensors
+    from .assembly import matinv_device
     dev = torch.device(device)
     m = field.mesh
     tri_ids = np.asarray(m.get_triangles(port_tags), dtype=np.int64)
@@ -159,7 +159,8 @@ def port_problem(field, er, ur, port_tags, basis, k0: float, pec_tags=(), target
     tet_of = np.asarray(m.tri_to_tet)[0, tri_ids]
     er_t = np.asarray(er)[:, :, tet_of]
     ur_t = np.asarray(ur)[:, :, tet_of]
-    Ms9 = np.ascontiguousarray(matinv_tensors(ur_t).reshape(9, nT))
+    Ms9 = matinv_device(torch.as_tensor(np.ascontiguousarray(np.asarray(ur_t, dtype=np.complex128).reshape(9, nT)),
+                                        device=dev))
     Mm9 = np.ascontiguousarray(np.asarray(er_t, dtype=np.complex128).reshape(9, nT))
     t = {k: torch.as_tensor(v, device=dev) for k, v in (("xy", xy), ("lem", np.ascontiguousarray(lem)),
                                                         ("Ms", Ms9), ("Mm", Mm9))}

@@ -98,6 +98,14 @@ int emg_assemble_tet_tensor_host(emg_plan* plan, const double* eps9, const doubl
 /* Releases the plan and its device memory. */
 void emg_plan_destroy(emg_plan* plan);
 
+/* matinv (fem/mth/optimized.py:440-461) of every tet's material tensor, on the device:
+ * the Ms = matinv(ur) that _matrix_builder passes to ned2_tet_stiff_mass
+ * (fem/physics/edm/optimized_assembly.py:98-105).  ncomp 9: s and out are complex
+ * (9, n_tets) DEVICE arrays (the reference's (3,3,n_tets) C order); a tensor with all
+ * off-diagonal entries zero gets its reciprocal diagonal, any other the reference's
+ * adj(s) * det(s).  ncomp 1: complex scalars (isotropic s * I), out = 1 / s. */
+int emg_matinv(int64_t n_tets, int ncomp, const double* s, double* out, void* stream);
+
 /* ------------------------------------------------------- surface terms ---
  * Replace the per-triangle Robin kernels behind assemble_robin_bc_excited /
  * assemble_robin_bc (fem/physics/edm/assembler.py:83-144).  One thread per
