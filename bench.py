@@ -482,7 +482,7 @@ def run_sweep(args):
     from emerge_gb300.freq import Assembler
     from emerge_gb300.geometry import iris_filter
     from emerge_gb300.solver import FrequencySweep
-    p = iris_filter(args.sweep_h)
+    p = iris_filter(args.sweep_h, hy=args.sweep_hy)
     asm = Assembler()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -761,7 +761,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=200_000, help="tets in the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the frequency-sweep measurement")
-    ap.add_argument("--sweep-h", type=float, default=2e-3, help="iris-filter mesh size (m)")
+    ap.add_argument("--sweep-h", type=float, default=2e-3, help="iris-filter mesh size across the guide (m)")
+    ap.add_argument("--sweep-hy", type=float, default=1.3e-3,
+                    help="iris-filter grid spacing along the guide (m): 1.3 mm gives ~3e5 DOFs at h = 2 mm")
     ap.add_argument("--sweep-points", type=int, default=401)
     ap.add_argument("--sweep-train", type=int, default=12, help="points solved first; their span gives the guesses")
     ap.add_argument("--sweep-mlp-train", type=int, default=32, help="training points of the MLP variant")

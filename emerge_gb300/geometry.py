@@ -85,7 +85,13 @@ CAVITIES = [15.8e-3, 17.6e-3, 18.0e-3, 17.6e-3, 15.8e-3]
 
 
 def iris_filter(h: float = 2e-3, a: float = 0.02286, b: float = 0.01016, t: float = 2e-3,
-                feed: float = 10e-3) -> Problem:
+                feed: float = 10e-3, hy: float | None = None) -> Problem:
+    """The five-cavity filter with grid spacing at most ``h`` across the guide and ``hy``
+    (default ``h``) along it.  Every element stays within the maximum element size
+    ``h``; a smaller ``hy`` adds cross-sections, which is how the structured grid reaches
+    the DOF count of a free mesh of the same maximum size (h = 2 mm, hy = 1.3 mm: about
+    3·10^5 DOFs)."""
+    hy = h if hy is None else hy
     # y positions of the iris slabs
     y = feed
     slabs = []
@@ -98,7 +104,7 @@ def iris_filter(h: float = 2e-3, a: float = 0.02286, b: float = 0.01016, t: floa
     ybreaks = sorted({0.0, L} | {s[0] for s in slabs} | {s[1] for s in slabs})
     xbreaks = sorted({0.0, a} | {(a - w) / 2 for w in IRIS_APERTURES} | {(a + w) / 2 for w in IRIS_APERTURES})
     xs = _lines(xbreaks, h)
-    ys = _lines(ybreaks, h)
+    ys = _lines(ybreaks, hy)
     zs = _lines([0.0, b], h)
 
     def metal(cx, cy, cz):
@@ -109,7 +115,8 @@ def iris_filter(h: float = 2e-3, a: float = 0.02286, b: float = 0.01016, t: floa
             m |= in_slab & outside
         return m.astype(np.int64)
 
-    return _guide_problem(xs, ys, zs, metal, a, b, L, f"5-cavity WR-90 iris filter, h={h * 1e3:.2f} mm")
+    name = f"5-cavity WR-90 iris filter, h={h * 1e3:.2f} mm" + (f", hy={hy * 1e3:.2f} mm" if hy != h else "")
+    return _guide_problem(xs, ys, zs, metal, a, b, L, name)
 
 
 TAG_GROUND, TAG_PATCH, TAG_FEED = 21, 22, 23
