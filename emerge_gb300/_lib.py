@@ -49,6 +49,8 @@ SIGNATURES = {
     "emg_segment_add": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_double, c_vp, c_vp]),
     "emg_combine": (ctypes.c_int, [c_i64, c_vp, c_vp, ctypes.c_double, c_vp, c_vp]),
     "emg_matinv": (ctypes.c_int, [c_i64, ctypes.c_int, c_vp, c_vp, c_vp]),
+    "emg_port_interp": (ctypes.c_int, [c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, ctypes.c_double,
+                                       ctypes.c_int, c_vp, c_vp]),
     "emg_rplan_create": (ctypes.c_int, [c_i64, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, ctypes.POINTER(c_vp)]),
     "emg_rplan_n": (c_i64, [c_vp]),
     "emg_rplan_nnz": (c_i64, [c_vp]),

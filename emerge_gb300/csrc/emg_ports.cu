@@ -194,3 +194,160 @@ extern "C" int emg_port_element_matrices(int64_t n_tris, const double* xy, const
     EMG_CUDA(cudaGetLastError());
     return EMG_OK;
 }
+
+// ------------------------------------------------------- port-mode fields ---
+// The Nedelec-Lagrange-2 field of a port mode at points of the port plane, the
+// counterpart of ned2_tri_interp_full (E) and ned2_tri_interp_curl (the H field up to
+// the factor j / (omega mu0)) of fem/mth/tri.py:228-401.  Thread per point, FP64.
+//
+// Point location as the reference: every triangle is tested, in order, with the local
+// coordinates from the inverse of [v2 - v1, v3 - v1] and the tolerances
+// xi >= -1e-6, eta >= -1e-6, xi + eta <= 1.00000001; the last triangle that contains the
+// point gives its value (the reference overwrites), a point in none gets zero.
+//
+// With the linear barycentric numerators l_i = a_i + b_i x + c_i y (tri_coefficients,
+// fem/mth/optimized.py:404-426: a_1 = x2 y3 - y2 x3, b_1 = y2 - y3, c_1 = x3 - x2 and
+// cyclic, all times the sign of the signed area; A = |area|) and the DOF values
+// e_1..e_14 of the triangle (tri_to_field order, the first eight times the lengths
+// L1 L2 L3 L3 L1 L2 L3 L1 of the edges (v0,v1), (v1,v2), (v0,v2)), write
+//   W_pq(u) = u_p l_q - u_q l_p      (u = b for the x component, c for the y component)
+// for the Whitney-type factor of the edge (p, q).  Then, with S = 8 A^3,
+//   E_u = [ e1 W12 l1 + e2 W23 l2 + e3 W13 l1 - e4 W13 l2 + e5 W12 l2 + e6 W23 l3
+//           + e7 W13 l3 + e8 W12 l3 ] / S,
+//   E_z = l1 [ (e9 + e10 + e11)(l1 - A) + (e12 + e13 + e14) l2 ] / (2 A^2),
+// and the curl terms are the reference's expressions for hx, hy, hz (the latter a
+// polynomial in a_i, b_i, c_i, x, y restated term by term below), each times the
+// corresponding diagonal entry of matinv(ur) of the triangle.
+namespace emg {
+namespace ports {
+
+__device__ __forceinline__ double2 cz(double r) { return make_double2(r, 0.0); }
+__device__ __forceinline__ double2 cm(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 cs(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__device__ __forceinline__ double2 ca(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csb(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+__global__ void k_port_interp(int64_t npts, const double* __restrict__ xy, int64_t nT, const int32_t* __restrict__ tris,
+                              int64_t nN, const double* __restrict__ nodes2, const int32_t* __restrict__ t2f,
+                              const double2* __restrict__ field, const double2* __restrict__ urinv, double beta,
+                              int which, double2* __restrict__ out) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npts; p += (int64_t)gridDim.x * blockDim.x) {
+        const double x = xy[p], y = xy[npts + p];
+        int64_t hit = -1;
+        for (int64_t t = 0; t < nT; ++t) {
+            const int32_t i1 = tris[t], i2 = tris[nT + t], i3 = tris[2 * nT + t];
+            const double x1 = nodes2[i1], y1 = nodes2[nN + i1];
+            const double m00 = nodes2[i2] - x1, m10 = nodes2[nN + i2] - y1;
+            const double m01 = nodes2[i3] - x1, m11 = nodes2[nN + i3] - y1;
+            const double det = m00 * m11 - m01 * m10;
+            if (det == 0.0) continue;
+            const double dx = x - x1, dy = y - y1;
+            const double xi = (m11 * dx - m01 * dy) / det, eta = (-m10 * dx + m00 * dy) / det;
+            if (xi + eta <= 1.00000001 && xi >= -1e-6 && eta >= -1e-6) hit = t;
+        }
+        double2 o0 = cz(0.0), o1 = cz(0.0), o2 = cz(0.0);
+        if (hit >= 0) {
+            const int64_t t = hit;
+            const int32_t v[3] = {tris[t], tris[nT + t], tris[2 * nT + t]};
+            double xs[3], ys[3];
+            for (int k = 0; k < 3; ++k) { xs[k] = nodes2[v[k]]; ys[k] = nodes2[nN + v[k]]; }
+            double a[3] = {xs[1] * ys[2] - ys[1] * xs[2], xs[2] * ys[0] - ys[2] * xs[0], xs[0] * ys[1] - ys[0] * xs[1]};
+            double b[3] = {ys[1] - ys[2], ys[2] - ys[0], ys[0] - ys[1]};
+            double c[3] = {xs[2] - xs[1], xs[0] - xs[2], xs[1] - xs[0]};
+            const double sA = 0.5 * ((xs[0] - xs[2]) * (ys[1] - ys[0]) - (xs[0] - xs[1]) * (ys[2] - ys[0]));
+            const double sg = sA > 0.0 ? 1.0 : (sA < 0.0 ? -1.0 : 0.0);
+            const double A = fabs(sA);
+            for (int k = 0; k < 3; ++k) { a[k] *= sg; b[k] *= sg; c[k] *= sg; }
+            const double L1 = sqrt((xs[0] - xs[1]) * (xs[0] - xs[1]) + (ys[0] - ys[1]) * (ys[0] - ys[1]));
+            const double L2 = sqrt((xs[1] - xs[2]) * (xs[1] - xs[2]) + (ys[1] - ys[2]) * (ys[1] - ys[2]));
+            const double L3 = sqrt((xs[0] - xs[2]) * (xs[0] - xs[2]) + (ys[0] - ys[2]) * (ys[0] - ys[2]));
+            const double mult[14] = {L1, L2, L3, L3, L1, L2, L3, L1, 1, 1, 1, 1, 1, 1};
+            double2 e[15];
+            for (int k = 0; k < 14; ++k) e[k + 1] = cs(mult[k], field[t2f[k * nT + t]]);
+            const double l1 = a[0] + b[0] * x + c[0] * y, l2 = a[1] + b[1] * x + c[1] * y, l3 = a[2] + b[2] * x + c[2] * y;
+            const double S = 8.0 * A * A * A;
+            // transverse components for u = b (x) and u = c (y)
+            auto trans = [&](const double* u) {
+                const double W12 = u[0] * l2 - u[1] * l1, W23 = u[1] * l3 - u[2] * l2, W13 = u[0] * l3 - u[2] * l1;
+                double2 s = cs(W12 * l1, e[1]);
+                s = ca(s, cs(W23 * l2, e[2]));
+                s = ca(s, cs(W13 * l1, e[3]));
+                s = csb(s, cs(W13 * l2, e[4]));
+                s = ca(s, cs(W12 * l2, e[5]));
+                s = ca(s, cs(W23 * l3, e[6]));
+                s = ca(s, cs(W13 * l3, e[7]));
+                s = ca(s, cs(W12 * l3, e[8]));
+                return s;
+            };
+            const double2 zs1 = ca(ca(e[9], e[10]), e[11]), zs2 = ca(ca(e[12], e[13]), e[14]);
+            const double2 zpoly = ca(cs(l1 - A, zs1), cs(l2, zs2));
+            if (which == 0) {
+                o0 = cs(1.0 / S, trans(b));
+                o1 = cs(1.0 / S, trans(c));
+                o2 = cs(l1 / (2.0 * A * A), zpoly);
+            } else {
+                const double2 jB = make_double2(0.0, beta);
+                const double2 gz_c = ca(cs(c[0], zs1), cs(c[1], zs2));
+                const double2 gz_b = ca(cs(b[0], zs1), cs(b[1], zs2));
+                const double2 hx = ca(cs(4.0 * A, ca(cs(c[0], zpoly), cs(l1, gz_c))), cm(jB, trans(c)));
+                const double2 hy = csb(cs(4.0 * A, ca(cs(b[0], zpoly), cs(l1, gz_b))), cm(jB, trans(b)));
+                // hz: the reference's polynomial (fem/mth/tri.py:392-393), grouped by DOF
+                const double a1 = a[0], a2 = a[1], a3 = a[2], b1 = b[0], b2 = b[1], b3 = b[2];
+                const double c1 = c[0], c2 = c[1], c3 = c[2];
+                double k1 = -3 * a1 * b1 * c2 + 3 * a1 * b2 * c1 - 3 * b1 * b1 * c2 * x + 3 * b1 * b2 * c1 * x
+                            - 3 * b1 * c1 * c2 * y + 3 * b2 * c1 * c1 * y;
+                double k2 = -3 * a2 * b2 * c3 + 3 * a2 * b3 * c2 - 3 * b2 * b2 * c3 * x + 3 * b2 * b3 * c2 * x
+                            - 3 * b2 * c2 * c3 * y + 3 * b3 * c2 * c2 * y;
+                double k3 = -3 * a1 * b1 * c3 + 3 * a1 * b3 * c1 - 3 * b1 * b1 * c3 * x + 3 * b1 * b3 * c1 * x
+                            - 3 * b1 * c1 * c3 * y + 3 * b3 * c1 * c1 * y;
+                double k4 = a1 * b2 * c3 - a1 * b3 * c2 + 2 * a2 * b1 * c3 - 2 * a2 * b3 * c1 + a3 * b1 * c2
+                            - a3 * b2 * c1 + 3 * b1 * b2 * c3 * x - 3 * b2 * b3 * c1 * x + 3 * b1 * c2 * c3 * y
+                            - 3 * b3 * c1 * c2 * y;
+                double k5 = -3 * a2 * b1 * c2 + 3 * a2 * b2 * c1 - 3 * b1 * b2 * c2 * x + 3 * b2 * b2 * c1 * x
+                            - 3 * b1 * c2 * c2 * y + 3 * b2 * c1 * c2 * y;
+                double k6 = -3 * a3 * b2 * c3 + 3 * a3 * b3 * c2 - 3 * b2 * b3 * c3 * x + 3 * b3 * b3 * c2 * x
+                            - 3 * b2 * c3 * c3 * y + 3 * b3 * c2 * c3 * y;
+                double k7 = -3 * a3 * b1 * c3 + 3 * a3 * b3 * c1 - 3 * b1 * b3 * c3 * x + 3 * b3 * b3 * c1 * x
+                            - 3 * b1 * c3 * c3 * y + 3 * b3 * c1 * c3 * y;
+                double k8 = a1 * b2 * c3 - a1 * b3 * c2 - a2 * b1 * c3 + a2 * b3 * c1 - 2 * a3 * b1 * c2
+                            + 2 * a3 * b2 * c1 - 3 * b1 * b3 * c2 * x + 3 * b2 * b3 * c1 * x - 3 * b1 * c2 * c3 * y
+                            + 3 * b2 * c1 * c3 * y;
+                double2 hz = cs(k1, e[1]);
+                hz = ca(hz, cs(k2, e[2]));
+                hz = ca(hz, cs(k3, e[3]));
+                hz = ca(hz, cs(k4, e[4]));
+                hz = ca(hz, cs(k5, e[5]));
+                hz = ca(hz, cs(k6, e[6]));
+                hz = ca(hz, cs(k7, e[7]));
+                hz = ca(hz, cs(k8, e[8]));
+                const double2 d0 = urinv[t], d1 = urinv[nT + t], d2 = urinv[2 * nT + t];
+                o0 = cm(cs(1.0 / S, hx), d0);
+                o1 = cm(cs(1.0 / S, hy), d1);
+                o2 = cm(cs(1.0 / S, hz), d2);
+            }
+        }
+        out[p] = o0;
+        out[npts + p] = o1;
+        out[2 * npts + p] = o2;
+    }
+}
+
+}  // namespace ports
+}  // namespace emg
+
+extern "C" int emg_port_interp(int64_t npts, const double* xy, int64_t n_tris, const int32_t* tris, int64_t n_nodes,
+                               const double* nodes2, const int32_t* tri_to_field, const double* field,
+                               const double* urinv_diag, double beta, int which, double* out, void* stream) {
+    using namespace emg;
+    EMG_CHECK_ARG(npts >= 0 && n_tris >= 0 && n_nodes >= 0, "emg_port_interp: negative size");
+    EMG_CHECK_ARG(which == 0 || which == 1, "emg_port_interp: which must be 0 (E) or 1 (curl)");
+    if (npts == 0) return EMG_OK;
+    EMG_CHECK_ARG(xy && out && (n_tris == 0 || (tris && nodes2 && tri_to_field && field)),
+                  "emg_port_interp: NULL array");
+    EMG_CHECK_ARG(which == 0 || n_tris == 0 || urinv_diag, "emg_port_interp: the curl needs urinv_diag");
+    ports::k_port_interp<<<grid_for(npts, 128), 128, 0, (cudaStream_t)stream>>>(
+        npts, xy, n_tris, tris, n_nodes, nodes2, tri_to_field, reinterpret_cast<const double2*>(field),
+        reinterpret_cast<const double2*>(urinv_diag), beta, which, reinterpret_cast<double2*>(out));
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}

@@ -208,3 +208,29 @@ def port_problem(field, er, ur, port_tags, basis, k0: float, pec_tags=(), target
         u = np.concatenate([ur_t[0, 0], ur_t[1, 1], ur_t[2, 2]])
         target_kz = float(np.mean(d.real) * np.mean(u.real) * 0.65 * k0)
     return PortProblem(As, Bs, solve_ids, S, float(target_kz))
+
+
+def port_field(surface: PortSurface, nodes_local: np.ndarray, field, pts_local: np.ndarray, which: int = 0,
+               urinv_diag: torch.Tensor | None = None, beta: float = 0.0) -> np.ndarray:
+    """The port-mode field at points of the port plane (``emg_port_interp``): ``which`` 0
+    gives E (ned2_tri_interp_full, fem/mth/tri.py:228-306), 1 the curl term of H
+    (ned2_tri_interp_curl, fem/mth/tri.py:308-401, without its factor j/(omega mu0)),
+    weighted by the diagonal of matinv(ur) per triangle (``urinv_diag``, (3, n_tris)
+    complex on the device).  Local coordinates in, (3, npts) complex local components out."""
+    field = torch.as_tensor(field)
+    dev = field.device if field.is_cuda else torch.device("cuda")
+    f = field.to(dev, torch.complex128).contiguous()
+    xy = torch.as_tensor(np.ascontiguousarray(pts_local, dtype=np.float64), device=dev)
+    nodes2 = torch.as_tensor(np.ascontiguousarray(nodes_local, dtype=np.float64), device=dev)
+    tris = torch.as_tensor(np.ascontiguousarray(surface.tris, dtype=np.int32), device=dev)
+    t2f = torch.as_tensor(np.ascontiguousarray(surface.tri_to_field, dtype=np.int32), device=dev)
+    npts = int(xy.shape[1])
+    out = torch.empty((3, npts), dtype=torch.complex128, device=dev)
+    ud = None if urinv_diag is None else urinv_diag.to(dev, torch.complex128).contiguous()
+    if which == 1 and ud is None:
+        raise ValueError("port_field: the curl needs urinv_diag")
+    with torch.cuda.device(dev):
+        _lib.call("emg_port_interp", npts, _vp(xy), int(tris.shape[1]), _vp(tris), int(nodes2.shape[1]),
+                  _vp(nodes2), _vp(t2f), _vp(f), _vp(ud) if ud is not None else None, ctypes.c_double(beta),
+                  int(which), _vp(out), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    return out.cpu().numpy()

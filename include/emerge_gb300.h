@@ -396,6 +396,19 @@ int emg_port_element_matrices(int64_t n_tris, const double* xy, const int32_t* l
                               const double* Mm9, double k0, int face_block, double* A_out, double* B_out,
                               void* stream);
 
+/* Field of a port mode at points of the port plane: ned2_tri_interp_full (which = 0,
+ * E) and ned2_tri_interp_curl (which = 1, the curl term of H without its factor
+ * j/(omega mu0)) of fem/mth/tri.py:228-401, as interpolate_Ef / interpolate_Hf of
+ * fem/elements/nedleg2.py:82-105 call them.  DEVICE arrays: xy (2, npts) local point
+ * coordinates; tris (3, n_tris) surface node ids; nodes2 (2, n_nodes) local node
+ * coordinates; tri_to_field (14, n_tris); field (n_field) complex; urinv_diag
+ * (3, n_tris) complex, the diagonal of matinv(ur) per triangle (which = 1 only); out
+ * (3, npts) complex local components.  The last triangle that contains a point gives
+ * its value, as in the reference; a point in none gets zero. */
+int emg_port_interp(int64_t npts, const double* xy, int64_t n_tris, const int32_t* tris, int64_t n_nodes,
+                    const double* nodes2, const int32_t* tri_to_field, const double* field, const double* urinv_diag,
+                    double beta, int which, double* out, void* stream);
+
 /* --------------------------------------------------------- far field ---
  * Stratton-Chu transform, the counterpart of stratton_chu_ff
  * (fem/physics/edm/sc.py:26-140).  Sources j < n_src at vis (3, n_src) f32 with

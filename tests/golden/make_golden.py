@@ -41,6 +41,8 @@ Fixtures:
   waveguide_diel.npz the guide with a lossy dielectric at port 1: SuperLU fields and the
                      S-parameters with the per-triangle material weight of the mode
                      integrals (fem/physics/edm/emfreq3d.py:767-778)
+  port_interp.npz    ned2_tri_interp_full / ned2_tri_interp_curl (fem/mth/tri.py:228-401) of
+                     random port fields on the WR-90 port face, at quadrature and random points
   farfield.npz       stratton_chu (fem/physics/edm/sc.py:143-180) of a short dipole's
                      near field sampled at the edge centres of a closed box surface
 """
@@ -394,6 +396,45 @@ def make_waveguide_diel():
     print(f"waveguide_diel: |S11|={abs(S[0, 0]):.4f} |S21|={abs(S[1, 0]):.4f} |S12|={abs(S[0, 1]):.4f}")
 
 
+def make_port_interp():
+    """ned2_tri_interp_full / ned2_tri_interp_curl (fem/mth/tri.py:228-401) of random port
+    fields on the WR-90 port face of waveguide.npz's mesh, at the 6-point quadrature points
+    of every face triangle and at random points of the face (local port coordinates)."""
+    from emerge_gb300.modes import port_surface
+    from emerge_gb300.bc import CoordinateSystem as PCS
+    z = np.load(os.path.join(HERE, "waveguide.npz"))
+    tri_ids = z["port_tris_1"].astype(np.int64)
+    mesh = type("M", (), {})()
+    mesh.tris = z["tris"].astype(np.int64)
+    S = port_surface(mesh, tri_ids)
+    a, b, L = (float(v) for v in z["dims"])
+    cs = PCS([1.0, 0, 0], [0, 0, 1.0], [0, -1.0, 0], [a / 2, 0.0, b / 2])
+    nodes = z["nodes"][:, S.node_ids]
+    xl, yl, _ = cs.in_local_cs(nodes[0], nodes[1], nodes[2])
+    nodes2 = np.stack([xl, yl])
+    rng = np.random.default_rng(21)
+    field = rng.normal(size=S.n_field) + 1j * rng.normal(size=S.n_field)
+    nT = S.tris.shape[1]
+    diadic = np.zeros((3, 3, nT), dtype=np.complex128)
+    for k in range(3):
+        diadic[k, k] = rng.uniform(0.5, 2, nT) + 1j * rng.uniform(-0.1, 0.1, nT)
+    D = ref_opt.gaus_quad_tri(4)
+    v = [nodes2[:, S.tris[k]] for k in range(3)]
+    qp = np.concatenate([v[0] * D[1, q] + v[1] * D[2, q] + v[2] * D[3, q] for q in range(D.shape[1])], axis=1)
+    rp = np.stack([rng.uniform(xl.min(), xl.max(), 200), rng.uniform(yl.min(), yl.max(), 200)])
+    coords = np.ascontiguousarray(np.concatenate([qp, rp], axis=1))
+    tris = np.ascontiguousarray(S.tris.astype(np.int64))
+    t2f = np.ascontiguousarray(S.tri_to_field.astype(np.int64))
+    Ex, Ey, Ez = ref_tri.ned2_tri_interp_full(coords, field, tris, np.ascontiguousarray(nodes2), t2f)
+    beta = 157.3
+    Hx, Hy, Hz = ref_tri.ned2_tri_interp_curl(coords, field, tris, np.ascontiguousarray(nodes2), t2f, diadic, beta)
+    np.savez_compressed(os.path.join(HERE, "port_interp.npz"), coords=coords, field=field, tris=S.tris.astype(np.int32),
+                        nodes2=nodes2, tri_to_field=S.tri_to_field.astype(np.int32),
+                        diadic_diag=np.stack([diadic[0, 0], diadic[1, 1], diadic[2, 2]]), beta=np.float64(beta),
+                        E=np.stack([Ex, Ey, Ez]), H=np.stack([Hx, Hy, Hz]))
+    print(f"port_interp: {coords.shape[1]} points over {nT} triangles")
+
+
 def make_waveguide_abc():
     """WR-90 guide with port 2 replaced by a first-order absorbing boundary
     (fem/bc.py:254-300, assemble_robin_bc fem/physics/edm/assembler.py:125-144)."""
@@ -647,7 +688,7 @@ def make_farfield():
 
 if __name__ == "__main__":
     which = _ARGS or ["tet", "tri", "small", "waveguide", "abc", "interp", "lumped", "frames", "port",
-                      "farfield", "waveguide_k", "waveguide_diel"]
+                      "farfield", "waveguide_k", "waveguide_diel", "port_interp"]
     if "tet" in which:
         make_tet_elements()
     if "tri" in which:
@@ -672,3 +713,5 @@ if __name__ == "__main__":
         make_waveguide_k()
     if "waveguide_diel" in which:
         make_waveguide_diel()
+    if "port_interp" in which:
+        make_port_interp()

@@ -127,3 +127,53 @@ def test_wr90_modes_match_oracle(cuda, face_block):
         assert abs(r.beta[0] - te10) / te10 <= 1e-5
     else:
         assert abs(r.beta[0] - 166.0238) / 166.0238 <= 1e-5
+
+
+@pytest.mark.gpu
+def test_port_field_interpolation_matches_reference(cuda):
+    """emg_port_interp against the reference's ned2_tri_interp_full (E) and
+    ned2_tri_interp_curl (the curl term of H, weighted by the diagonal of matinv(ur)) on
+    random port fields of the WR-90 port face: 1e-12 of the largest value."""
+    import types
+    import torch
+    from emerge_gb300.modes import port_field
+    z = load("port_interp.npz")
+    S = types.SimpleNamespace(tris=z["tris"], tri_to_field=z["tri_to_field"])
+    ud = torch.as_tensor(z["diadic_diag"], device="cuda")
+    E = port_field(S, z["nodes2"], z["field"], z["coords"], 0)
+    H = port_field(S, z["nodes2"], z["field"], z["coords"], 1, ud, float(z["beta"]))
+    assert _rel(E, z["E"]) <= 1e-12
+    assert _rel(H, z["H"]) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_modal_port_sweep_matches_rectangular_waveport(cuda):
+    """ModalPort (mode solved on the port face, normalised to unit power, beta(k0) from the
+    solved mode) against the analytic TE10 RectangularWaveguide on the same WR-90 mesh.
+    With the integrated face block the solved TE10 constant is the analytic one, so S21
+    and S11 agree to the discretisation of the mode shape."""
+    from emerge_gb300.bc import ModalPort
+    from emerge_gb300.freq import Assembler
+    from emerge_gb300.geometry import straight_waveguide
+    from emerge_gb300.solver import FrequencySweep
+    p = straight_waveguide(3e-3)
+    rect = [bc for bc in p.bcs if hasattr(bc, "port_number")]
+    pec = [bc for bc in p.bcs if not hasattr(bc, "port_number")]
+    pec_tags = [t for bc in pec for t in bc.tags]
+    modal = []
+    for r in rect:
+        mp = ModalPort(r.tags, r.port_number, cs=r.cs)
+        modes = mp.modal_analysis(p.field, p.er, p.ur, 10e9, pec_tags=pec_tags, nmodes=1, face_block=True)
+        assert len(modes) == 1 and modes[0].modetype == "TE"
+        te10 = np.sqrt((2 * np.pi * 10e9 / 299792458) ** 2 - (np.pi / 0.02286) ** 2)
+        assert abs(modes[0].beta - te10) / te10 < 1e-4
+        assert abs(abs(modes[0].power) * modes[0].norm_factor ** 2 - 1) < 1e-12
+        modal.append(mp)
+    freqs = np.array([9.0e9, 10.0e9, 11.0e9])
+    r_rect = FrequencySweep(Assembler(), p.field, p.er, p.ur, p.bcs).run(freqs, method="plain", precond="slab64",
+                                                                          tol=1e-11)
+    r_modal = FrequencySweep(Assembler(), p.field, p.er, p.ur, pec + modal).run(freqs, method="plain",
+                                                                                precond="slab64", tol=1e-11)
+    assert np.all(r_modal.residuals <= 1e-10)
+    assert np.max(np.abs(np.abs(r_modal.S) - np.abs(r_rect.S))) <= 2e-3
+    assert np.all(np.abs(np.abs(r_modal.S[:, 1, 0]) - 1) <= 5e-3)
