@@ -5,8 +5,8 @@
 port_vector, solve_ids, reuse)`` per (frequency, port), ports in boundary-condition
 order, ``reuse`` False on the first port of each frequency.  Solutions within 1e-6 of
 the reference's SuperLU fields.  ``GPUEigSolver`` against SciPy's dense generalized eig
-with the reference's mode filter (the LAPACK slot) and against ARPACK shift-invert
-(the ARPACK slot) on the WR-90 port problem.
+with the reference's mode filter (the LAPACK slot) and against the dense eigenvalue
+nearest the shift (the ARPACK slot) on the WR-90 port problem.
 """
 import numpy as np
 import pytest
@@ -94,19 +94,24 @@ def test_eig_solver_direct_slot_matches_lapack_filter(torch_cuda):
         assert np.linalg.norm(A @ v - lam_g[i] * (B @ v)) <= 1e-8 * np.linalg.norm(A @ v)
 
 
-def test_eig_solver_iterative_slot_matches_arpack(torch_cuda):
-    """The ARPACK slot: the eigenvalue nearest sigma = -target_k0^2 (TE10; the next nearest
-    ones are the problem's degenerate zero eigenvalues)."""
+def test_eig_solver_iterative_slot_nearest_eigenvalue(torch_cuda):
+    """The ARPACK slot: the eigenvalue nearest sigma = -target_k0^2, against the dense
+    generalized eigenvalues of the same pencil (TE10; the next nearest ones are the
+    pencil's degenerate zero eigenvalues).  SciPy's ARPACK shift-invert is not the check
+    here: on this pencil it returns complex values that are not eigenvalues of it."""
+    import scipy.linalg
     import scipy.sparse as sp
-    import scipy.sparse.linalg as spla
     from emerge_gb300.routine import GPUEigSolver
     k0 = 2 * np.pi * 10e9 / 299792458
     pp = _port_problem(k0)
-    A, B = sp.csr_matrix(pp.A.cpu().numpy()), sp.csr_matrix(pp.B.cpu().numpy())
+    Ad, Bd = pp.A.cpu().numpy(), pp.B.cpu().numpy()
+    A, B = sp.csr_matrix(Ad), sp.csr_matrix(Bd)
     t = pp.target_kz
     lam_g, vec_g = GPUEigSolver(iterative=True).eig(A, B, 1, t, "LM")
-    lam = spla.eigs(A.tocsc(), k=1, M=B.tocsc(), sigma=-t * t, which="LM", return_eigenvectors=False)
+    lam = scipy.linalg.eig(Ad, Bd, right=False)
+    lam = lam[np.isfinite(lam)]
+    near = lam[np.argmin(np.abs(lam + t * t))]
     assert len(lam_g) == 1 and lam_g[0] < -1
-    assert abs(lam_g[0] - lam[0].real) / abs(lam[0].real) <= 1e-8
+    assert abs(lam_g[0] - near.real) / abs(near.real) <= 1e-8
     v = vec_g[:, 0]
     assert np.linalg.norm(A @ v - lam_g[0] * (B @ v)) <= 1e-8 * np.linalg.norm(A @ v)
