@@ -851,8 +851,15 @@ __global__ void k_ent_desc(const int32_t* __restrict__ gents, int64_t n, const i
 // Re B and Im B and writes E and B (Im E = 0); IM = true, launched after it, returns at
 // once unless some tet's mu^-1 is complex, and then accumulates Im E and writes it.
 constexpr int kAcc = 3;                 // accumulators per (row, position)
+constexpr int kRing = 4;                // tets in flight per warp (prefetch distance kRing - 1)
+struct __align__(16) RingSlot {
+    float4 col[20][2];                  // the staged unit of each column: (D0, D1), (F0, F1)
+    float4 sc[2];                       // the tet's material scales
+    uint32_t pos[8];                    // the 20 CSR positions (bytes), padded
+};
 struct __align__(16) OwnSm {
     float2 acc[2 * kNmax * kAcc];       // [row][position][component] compensated (s, e)
+    RingSlot ring[kRing];
     EntDesc ed[kGmax];
     int64_t iidx[kKmax];                // incidence index of each step
     int32_t tet[kKmax];
@@ -873,6 +880,38 @@ __device__ __forceinline__ void acc_sm(float2& c, df x, df y) {   // c += x * y
     const float err = __fadd_rn(__fsub_rn(c.x, __fsub_rn(t, bb)), __fsub_rn(p, bb));
     c.y = __fadd_rn(c.y, __fadd_rn(err, pe));
     c.x = t;
+}
+
+__device__ __forceinline__ void cp16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp4(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Asynchronous copies of step i's data into ring slot i % kRing: lane c < 20 its staged
+// column unit, lanes 20-21 the tet's scales, lanes 22-26 the 20 position bytes.  Every
+// lane commits one group per step (empty for idle lanes), so group counts stay aligned.
+__device__ __forceinline__ void ring_issue(RingSlot& r, const float4* __restrict__ st, const float4* __restrict__ tscale,
+                                           const uint8_t* __restrict__ ipos, int64_t t, int slot, int64_t iidx,
+                                           int lane, bool im) {
+    if (lane < 20) {
+        const float4* u = st + st_unit(t, slot, lane) * 2;
+        cp16(&r.col[lane][0], u);
+        if (!im) cp16(&r.col[lane][1], u + 1);
+    } else if (lane < 22) {
+        cp16(&r.sc[lane - 20], tscale + 2 * t + (lane - 20));
+    } else if (lane < 27) {
+        cp4(&r.pos[lane - 22], ipos + iidx * 20 + 4 * (lane - 22));
+    }
+    cp_commit();
 }
 
 template <bool IM>
@@ -918,30 +957,23 @@ __global__ void __launch_bounds__(32 * kOwnWarps) k_fill_st(const float4* __rest
         }
         for (int i = lane; i < 2 * nmax * nc; i += 32) sm.acc[i] = make_float2(0.f, 0.f);
         __syncwarp();
-        float4 cd = {}, cf = {}, cse = {}, csb = {}, nd = {}, nf = {}, nse = {}, nsb = {};
-        int cp = 0, np = 0;
-        if (lane < 20) {
-            const int64_t t = sm.tet[0];
-            const float4* r = st + st_unit(t, sm.slot[0], lane) * 2;
-            cd = __ldg(r);
-            if (!IM) cf = __ldg(r + 1);
-            cse = __ldg(tscale + 2 * t);
-            if (!IM) csb = __ldg(tscale + 2 * t + 1);
-            cp = __ldg(ipos + sm.iidx[0] * 20 + lane);
+        for (int i = 0; i < kRing - 1; ++i) {
+            if (i < ktot) ring_issue(sm.ring[i], st, tscale, ipos, sm.tet[i], sm.slot[i], sm.iidx[i], lane, IM);
+            else cp_commit();
         }
         for (int i = 0; i < ktot; ++i) {
             const int u = sm.ent[i];
             const int n = sm.ed[u].n;
+            const int ip = i + kRing - 1;
+            if (ip < ktot) ring_issue(sm.ring[ip % kRing], st, tscale, ipos, sm.tet[ip], sm.slot[ip], sm.iidx[ip], lane, IM);
+            else cp_commit();
+            cp_wait<kRing - 1>();
+            __syncwarp();
+            const RingSlot& r = sm.ring[i % kRing];
             if (lane < 20) {
-                if (i + 1 < ktot) {
-                    const int64_t t = sm.tet[i + 1];
-                    const float4* r = st + st_unit(t, sm.slot[i + 1], lane) * 2;
-                    nd = __ldg(r);
-                    if (!IM) nf = __ldg(r + 1);
-                    nse = __ldg(tscale + 2 * t);
-                    if (!IM) nsb = __ldg(tscale + 2 * t + 1);
-                    np = __ldg(ipos + sm.iidx[i + 1] * 20 + lane);
-                }
+                const int cp = reinterpret_cast<const uint8_t*>(r.pos)[lane];
+                const float4 cd = r.col[lane][0];
+                const float4 cse = r.sc[0];
                 float2* c0 = sm.acc + cp * nc;
                 float2* c1 = sm.acc + (n + cp) * nc;
                 const df D0 = mk(cd.x, cd.y), D1 = mk(cd.z, cd.w);
@@ -949,6 +981,8 @@ __global__ void __launch_bounds__(32 * kOwnWarps) k_fill_st(const float4* __rest
                     acc_sm(c0[0], mk(cse.z, cse.w), D0);
                     acc_sm(c1[0], mk(cse.z, cse.w), D1);
                 } else {
+                    const float4 cf = r.col[lane][1];
+                    const float4 csb = r.sc[1];
                     const df F0 = mk(cf.x, cf.y), F1 = mk(cf.z, cf.w);
                     acc_sm(c0[0], mk(cse.x, cse.y), D0);
                     acc_sm(c1[0], mk(cse.x, cse.y), D1);
@@ -959,7 +993,6 @@ __global__ void __launch_bounds__(32 * kOwnWarps) k_fill_st(const float4* __rest
                 }
             }
             __syncwarp();
-            cd = nd; cf = nf; cse = nse; csb = nsb; cp = np;
             if (i + 1 == ktot || sm.ent[i + 1] != u) {
                 const EntDesc& ed = sm.ed[u];
                 for (int x = lane; x < 2 * n; x += 32) {
