@@ -58,7 +58,7 @@ __device__ __forceinline__ double2 to_d(double2 v) { return v; }
 
 constexpr int kTile = 64;          // Gauss-Jordan tile and GEMM output tile
 constexpr int kThreads = 256;
-constexpr int kDiagThreads = 1024;  // pivot-tile inversion: 4 rows per thread
+constexpr int kDiagThreads = 256;   // pivot-tile inversion: a 4 x 4 block per thread
 constexpr int kMaxRows = 16;       // rows per CTA in the Schur-complement kernel
 constexpr int kSchurSmem = 200 * 1024;
 constexpr int64_t kMaxWidth = 12288;
@@ -201,161 +201,175 @@ __global__ void __launch_bounds__(kThreads) k_schur(int64_t wp, int64_t w, int64
     }
 }
 
-// In-place inverse of pivot tile k (tb x tb) with partial pivoting inside the tile;
-// the inverse also goes to pinv (ld 64).  Grid 1 x 1 x F.
-//
-// Gauss-Jordan on a 64 x 64 shared tile (padded with the identity when tb < 64),
-// two barriers per pivot.  Thread t owns column t % 64 and rows t / 64 + 16q, so a
-// warp touches 32 consecutive columns of one row (no bank conflicts); 1024 threads
-// keep enough warps per scheduler to hide the update's instruction latencies.  Step c:
-// every thread reduces the 16 pivot candidates of column c (one per owner
-// thread, largest |a_rc| below the diagonal, lowest row on ties); (S) the pivot
-// row p is swapped into row c while the scaled pivot row and the old column c are
-// formed; (U) rank-1 update from registers, during which the owners of column
-// c+1 leave their candidates for the next step.  The row swaps become one column
-// permutation at the end.
 template <typename T> __device__ __forceinline__ T crecip(T v) {
     const auto m2 = v.x * v.x + v.y * v.y;
     return mk(v.x / m2, -v.y / m2);
 }
 
+// In-place inverse of pivot tile k (tb x tb, padded with the identity when tb < 64)
+// with partial pivoting inside the tile; the inverse also goes to pinv (ld 64).
+// Grid 1 x 1 x F.  Gauss-Jordan: pivot = largest |a_rc| on or below the diagonal, the
+// lower row on ties; pivots at or below rel_thr * max|a| are replaced by that
+// threshold and counted; the row swaps are applied as one column permutation at the
+// end.  256 threads as a 16 x 16 grid: thread (ty, tx) holds rows ty + 16 i and
+// columns tx + 16 j (i, j < 4) of the tile in registers.  Step c: (S) the owners of
+// row p, of row c and of column c leave them in shared memory; (U) every thread forms
+// the scaled pivot row for its columns and updates its 16 entries, the owners of
+// column c + 1 leave their candidates.  Two barriers per pivot, no tile in shared
+// memory.
 template <typename R>
 __global__ void __launch_bounds__(kDiagThreads) k_gj_diag(int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
-                                                      int64_t totD, int64_t offD, typename C2<R>::T* __restrict__ pinv,
-                                                      R rel_thr, int32_t* __restrict__ perturbed) {
+                                                         int64_t totD, int64_t offD, typename C2<R>::T* __restrict__ pinv,
+                                                         R rel_thr, int32_t* __restrict__ perturbed) {
     using T = typename C2<R>::T;
-    constexpr int kQ = kTile * kTile / kDiagThreads;   // rows per thread
-    constexpr int kRowStep = kDiagThreads / kTile;     // row stride between a thread's rows
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T(*a)[kTile + 1] = reinterpret_cast<T(*)[kTile + 1]>(smem_raw);
-    __shared__ T rowc[kTile], colc[kTile];
-    __shared__ int piv[kTile], perm[kTile];
-    __shared__ R cand_m[kDiagThreads / kTile];
-    __shared__ int cand_i[kDiagThreads / kTile];
-    __shared__ T cand_v[kDiagThreads / kTile];
+    __shared__ T prow[kTile], orow[kTile], colc[kTile];
+    __shared__ R cand_m[16];
+    __shared__ int cand_i[16];
+    __shared__ int piv[kTile], perm[kTile], iperm[kTile];
     __shared__ R s_red[kDiagThreads / 32];
     const int64_t f = blockIdx.z;
     T* M = Sinv + f * totD + offD;
     const int64_t k0 = (int64_t)k * kTile;
     const int tb = (int)min((int64_t)kTile, w - k0);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int j = tid % kTile, r0 = tid / kTile, slot = r0;
+    const int ty = tid >> 4, tx = tid & 15;
+    T a[4][4];
     R mx = 0;
-    for (int idx = tid; idx < kTile * kTile; idx += kDiagThreads) {
-        const int r = idx / kTile, c = idx % kTile;
-        T v;
-        if (r < tb && c < tb) {
-            v = M[(k0 + r) * w + k0 + c];
-            mx = max(mx, v.x * v.x + v.y * v.y);
-        } else {
-            v = mk((R)(r == c ? 1 : 0), (R)0);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = ty + 16 * i, cc = tx + 16 * j;
+            T v;
+            if (r < tb && cc < tb) {
+                v = M[(k0 + r) * w + k0 + cc];
+                mx = max(mx, v.x * v.x + v.y * v.y);
+            } else {
+                v = mk((R)(r == cc ? 1 : 0), (R)0);
+            }
+            a[i][j] = v;
         }
-        a[r][c] = v;
-    }
 #pragma unroll
     for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) s_red[wid] = mx;
+    if (tx == 0) {   // candidates of column 0
+        R bm = -1;
+        int bi = kTile;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = ty + 16 * i;
+            const R m2 = a[i][0].x * a[i][0].x + a[i][0].y * a[i][0].y;
+            if (r < tb && m2 > bm) { bm = m2; bi = r; }
+        }
+        cand_m[ty] = bm;
+        cand_i[ty] = bi;
+    }
     __syncthreads();
     R thr2 = 0;
 #pragma unroll
     for (int i = 0; i < kDiagThreads / 32; ++i) thr2 = max(thr2, s_red[i]);
     thr2 *= rel_thr * rel_thr;   // |pivot|^2 at or below this is replaced
-    // candidates of column 0 from shared memory
-    if (j == 0) {
-        R best = -1;
-        int bi = kTile;
-        T bv = mk((R)0, (R)0);
-#pragma unroll
-        for (int q = 0; q < kQ; ++q) {
-            const int r = r0 + kRowStep * q;
-            if (r < tb) {
-                const T v = a[r][0];
-                const R m2 = v.x * v.x + v.y * v.y;
-                if (m2 > best) { best = m2; bi = r; bv = v; }
-            }
-        }
-        cand_m[slot] = best; cand_i[slot] = bi; cand_v[slot] = bv;
-    }
-    __syncthreads();
-    T v[kQ];
     for (int c = 0; c < tb; ++c) {
-        // pivot of column c from the four candidates (same result in every thread)
         R best = cand_m[0];
         int p = cand_i[0];
-        T pv = cand_v[0];
 #pragma unroll
-        for (int i = 1; i < kDiagThreads / kTile; ++i) {
+        for (int i = 1; i < 16; ++i) {
             const R m2 = cand_m[i];
             const int ii = cand_i[i];
-            if (m2 > best || (m2 == best && ii < p)) { best = m2; p = ii; pv = cand_v[i]; }
+            if (m2 > best || (m2 == best && ii < p)) { best = m2; p = ii; }
         }
-        if (!(best > thr2)) {   // also catches a zero column
-            pv = mk(thr2 > 0 ? (R)sqrt(thr2) : (R)1, (R)0);
-            if (tid == 0) atomicAdd(perturbed + f, 1);
-        }
+        const bool small = !(best > thr2);   // also catches a zero column
         if (p >= tb) p = c;
-        const T inv = crecip(pv);
-        if (tid < kTile) {
-            const T vp = a[p][tid];
-            if (p != c) a[p][tid] = a[c][tid];
-            rowc[tid] = cmul(vp, inv);
-            if (tid == 0) piv[c] = p;
-        } else if (tid < 2 * kTile) {
-            const int r = tid - kTile;
-            colc[r] = r == p ? a[c][c] : a[r][c];
+        // (S) row p, row c and column c into shared memory
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = ty + 16 * i;
+            if (r == p) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) prow[tx + 16 * j] = a[i][j];
+            }
+            if (r == c && p != c) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) orow[tx + 16 * j] = a[i][j];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (tx + 16 * j == c) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) colc[ty + 16 * i] = a[i][j];
+            }
+        if (tid == 0) {
+            piv[c] = p;
+            if (small) atomicAdd(perturbed + f, 1);
         }
         __syncthreads();
-        const T rj = rowc[j];
+        // (U) rank-1 update; row c becomes the scaled pivot row, row p the old row c
+        const T pv = small ? mk(thr2 > 0 ? (R)sqrt(thr2) : (R)1, (R)0) : prow[c];
+        const T inv = crecip(pv);
+        T rj[4];
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) v[q] = a[r0 + kRowStep * q][j];
+        for (int j = 0; j < 4; ++j) rj[j] = cmul(prow[tx + 16 * j], inv);
+        const int cn = c + 1;
+        R bm = -1;
+        int bi = kTile;
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) {
-            const int r = r0 + kRowStep * q;
-            const T cr = colc[r];
+        for (int i = 0; i < 4; ++i) {
+            const int r = ty + 16 * i;
             if (r == c) {
-                v[q] = j == c ? inv : rj;
-            } else if (j == c) {
-                const T t = cmul(cr, inv);
-                v[q] = mk(-t.x, -t.y);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) a[i][j] = (tx + 16 * j == c) ? inv : rj[j];
             } else {
-                const T t = cmul(cr, rj);
-                v[q].x -= t.x;
-                v[q].y -= t.y;
-            }
-        }
+                const bool isp = r == p;
+                const T cr = isp ? colc[c] : colc[r];
 #pragma unroll
-        for (int q = 0; q < kQ; ++q) a[r0 + kRowStep * q][j] = v[q];
-        if (j == c + 1) {
-            R bm = -1;
-            int bi = kTile;
-            T bv = mk((R)0, (R)0);
-#pragma unroll
-            for (int q = 0; q < kQ; ++q) {
-                const int r = r0 + kRowStep * q;
-                if (r > c && r < tb) {
-                    const R m2 = v[q].x * v[q].x + v[q].y * v[q].y;
-                    if (m2 > bm) { bm = m2; bi = r; bv = v[q]; }
+                for (int j = 0; j < 4; ++j) {
+                    const int cc = tx + 16 * j;
+                    T v = isp ? orow[cc] : a[i][j];
+                    if (cc == c) {
+                        const T t = cmul(cr, inv);
+                        v = mk(-t.x, -t.y);
+                    } else {
+                        const T t = cmul(cr, rj[j]);
+                        v.x -= t.x;
+                        v.y -= t.y;
+                    }
+                    a[i][j] = v;
+                    if (cc == cn && r > c && r < tb) {
+                        const R m2 = v.x * v.x + v.y * v.y;
+                        if (m2 > bm) { bm = m2; bi = r; }
+                    }
                 }
             }
-            cand_m[slot] = bm; cand_i[slot] = bi; cand_v[slot] = bv;
+        }
+        if (tx == (cn & 15)) {
+            cand_m[ty] = bm;
+            cand_i[ty] = bi;
         }
         __syncthreads();
     }
-    if (tid == 0) {
+    if (tid == 0) {   // the swaps in reverse give the column permutation; iperm is its inverse
         for (int c = 0; c < kTile; ++c) perm[c] = c;
         for (int c = tb - 1; c >= 0; --c) {
             const int q = piv[c];
             if (q != c) { const int t = perm[c]; perm[c] = perm[q]; perm[q] = t; }
         }
+        for (int c = 0; c < kTile; ++c) iperm[perm[c]] = c;
     }
     __syncthreads();
+    // column cc of the unpermuted inverse is column iperm[cc] of the result
     T* P = pinv + f * kTile * kTile;
-    for (int idx = tid; idx < tb * tb; idx += kDiagThreads) {
-        const int r = idx / tb, c = idx % tb;
-        const T x = a[r][perm[c]];
-        M[(k0 + r) * w + k0 + c] = x;
-        P[r * kTile + c] = x;
-    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = ty + 16 * i, cc = tx + 16 * j;
+            if (r < tb && cc < tb) {
+                const int cd = iperm[cc];
+                M[(k0 + r) * w + k0 + cd] = a[i][j];
+                P[r * kTile + cd] = a[i][j];
+            }
+        }
 }
 
 // mode 0: row panel  M[k, c] = Pinv M[k, c]       (grid: column tiles x 1 x F, c != k)
@@ -985,9 +999,7 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
         k_offvals<R><<<grid_for(s->nU * F, 256), 256, 0, st>>>(s->nU, Bm, F, amat, A, s->ucsrc, static_cast<T*>(s->UCval));
     }
     EMG_CUDA(cudaGetLastError());
-    const int diag_smem = (int)(sizeof(T) * kTile * (kTile + 1));
     EMG_CUDA(cudaFuncSetAttribute(k_schur<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSchurSmem));
-    EMG_CUDA(cudaFuncSetAttribute(k_gj_diag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, diag_smem));
     const R rel_thr = sizeof(R) == 4 ? (R)1e-6 : (R)1e-13;
     for (int i = 0; i < s->m; ++i) {
         const int64_t w = s->off[i + 1] - s->off[i];
@@ -1007,9 +1019,8 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
             EMG_CUDA(cudaMemcpy2DAsync(Scopy, sizeof(T) * sq, Sinv + s->offD[i], sizeof(T) * s->totD, sizeof(T) * w * w,
                                        (size_t)F, cudaMemcpyDeviceToDevice, st));
         for (int k = 0; k < nt; ++k) {
-            k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kDiagThreads, diag_smem, st>>>(w, k, Sinv, s->totD, s->offD[i],
-                                                                             static_cast<T*>(s->pinv), rel_thr,
-                                                                             s->perturbed);
+            k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kDiagThreads, 0, st>>>(w, k, Sinv, s->totD, s->offD[i],
+                                                                      static_cast<T*>(s->pinv), rel_thr, s->perturbed);
             if (nt > 1) {
                 const T* P = static_cast<const T*>(s->pinv);
                 k_gj_panel<R><<<dim3(nt, 1, (unsigned)F), kThreads, 0, st>>>(0, w, k, Sinv, s->totD, s->offD[i], P);
