@@ -72,6 +72,7 @@ SIGNATURES = {
                                             ctypes.c_int, ctypes.c_double, ctypes.c_double, c_vp, c_vp, c_vp, c_vp]),
     "emg_tc_gemm_tf32": (ctypes.c_int, [c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp]),
     "emg_slab_set_tensor_cores": (ctypes.c_int, [c_vp, ctypes.c_int]),
+    "emg_slab_set_factor_tensor_cores": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "emg_slab_set_wide_group": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "emg_slab_set_max_splits": (ctypes.c_int, [c_vp, ctypes.c_int]),
     "emg_field_interp": (ctypes.c_int, [c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp,

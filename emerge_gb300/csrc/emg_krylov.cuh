@@ -71,6 +71,14 @@ int tc_slab_product(int64_t w, int64_t row0, int64_t Bc, const void* groups, int
                     int64_t totD, int64_t offD, const float2* Y, float alpha, int beta, float2* Out, int32_t* status,
                     cudaStream_t st);
 
+// Rank-64 update of Gauss-Jordan step k on the tcgen05 tensor cores in FP32-equivalent
+// precision (split-TF32 products, FP32 accumulation; emg_tc.cu): M[r, c] -= M[r, K]
+// M[K, c] for the F complex64 w x w blocks Sinv + f totD + offD, rows and columns of
+// tile k excluded, tile (la, la) excluded when la >= 0; status (device) set to 1 if a
+// bounded wait ran out.
+int tc_gj_update(int64_t w, int k, int la, int64_t F, float2* Sinv, int64_t totD, int64_t offD, int32_t* status,
+                 cudaStream_t st);
+
 // Preconditioner on FP32 vectors (the inner solves of the mixed-precision refinement).
 struct Precond32 {
     virtual ~Precond32() = default;

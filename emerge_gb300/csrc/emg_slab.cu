@@ -201,32 +201,155 @@ __global__ void __launch_bounds__(kThreads) k_schur(int64_t wp, int64_t w, int64
     }
 }
 
-template <typename T> __device__ __forceinline__ T crecip(T v) {
-    const auto m2 = v.x * v.x + v.y * v.y;
-    return mk(v.x / m2, -v.y / m2);
-}
-
 // In-place inverse of pivot tile k (tb x tb, padded with the identity when tb < 64)
 // with partial pivoting inside the tile; the inverse also goes to pinv (ld 64).
 // Grid 1 x 1 x F.  Gauss-Jordan: pivot = largest |a_rc| on or below the diagonal, the
-// lower row on ties; pivots at or below rel_thr * max|a| are replaced by that
-// threshold and counted; the row swaps are applied as one column permutation at the
-// end.  256 threads as a 16 x 16 grid: thread (ty, tx) holds rows ty + 16 i and
-// columns tx + 16 j (i, j < 4) of the tile in registers.  Step c: (S) the owners of
-// row p, of row c and of column c leave them in shared memory; (U) every thread forms
-// the scaled pivot row for its columns and updates its 16 entries, the owners of
-// column c + 1 leave their candidates.  Two barriers per pivot, no tile in shared
-// memory.
+// lower row on ties (magnitudes compared in FP32); pivots with |a|^2 at or below
+// rel_thr^2 max|a|^2 are replaced by that threshold and counted; the row swaps are
+// applied as one column permutation at the end.
+//
+// 256 threads as a 16 x 16 grid: thread (ty, tx) holds rows ty + 16 i and columns
+// tx + 16 j (i, j < 4) of the tile in registers.  The pivot loop runs over four
+// column blocks of 16 with the block index a compile-time constant, so the pivot
+// column and row sit at fixed register positions.  Step c:
+//   (S) the owners of row p and row c leave them in shared memory, the owners of
+//       column c leave it with rows c and p exchanged, the owner of a_pc forms the
+//       reciprocal of the pivot;
+//   (U) the owners of row p take the old row c; column c becomes the identity column
+//       and row c of the multiplier row the reciprocal, so one rank-1 update forms
+//       both the eliminated entries and the new column c; row c takes the scaled
+//       pivot row; the owners of column c + 1 (two lanes per warp) reduce their rows
+//       to one packed (|a|^2, row) key per warp.
+// Two barriers per pivot, no tile in shared memory.
+template <typename T> __device__ __forceinline__ T crecip(T v);
+template <> __device__ __forceinline__ float2 crecip<float2>(float2 v) {
+    const float s = __frcp_rn(v.x * v.x + v.y * v.y);
+    return make_float2(v.x * s, -v.y * s);
+}
+template <> __device__ __forceinline__ double2 crecip<double2>(double2 v) {
+    const double s = __drcp_rn(v.x * v.x + v.y * v.y);
+    return make_double2(v.x * s, -v.y * s);
+}
+
+// (|a|^2 as FP32 bits, 63 - row): the unsigned maximum is the largest magnitude, then the lowest row
+template <typename R> __device__ __forceinline__ unsigned long long pivot_key(R m2, int r) {
+    return ((unsigned long long)__float_as_uint((float)m2) << 32) | (unsigned)(63 - r);
+}
+
+template <typename R> struct DiagShared {
+    using T = typename C2<R>::T;
+    T prow[kTile], orow[kTile], colc[kTile];
+    unsigned long long cand[kDiagThreads / 32];
+    int piv[kTile], perm[kTile], iperm[kTile];
+    R red[kDiagThreads / 32];
+    T inv;
+};
+
+// the key of the best row r > rmin (r < tb) of column 16 JN + tx among this thread's
+// rows, combined over lanes tx and tx + 16; lane tx (== column % 16) stores it
+template <int JN, typename R>
+__device__ __forceinline__ void diag_candidates(const typename C2<R>::T (&a)[4][4], int cn, int rmin, int tb,
+                                                DiagShared<R>& sh) {
+    const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 4, tx = tid & 15;
+    unsigned long long key = 0;
+    if (tx == (cn & 15)) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = ty + 16 * i;
+            const R m2 = a[i][JN].x * a[i][JN].x + a[i][JN].y * a[i][JN].y;
+            const unsigned long long kk = (r > rmin && r < tb) ? pivot_key<R>(m2, r) : 0ull;
+            key = kk > key ? kk : key;
+        }
+    }
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, key, 16);
+    key = o > key ? o : key;
+    if (lane == (cn & 15)) sh.cand[tid >> 5] = key;
+}
+
+template <int JC, typename R>
+__device__ __forceinline__ void diag_block(typename C2<R>::T (&a)[4][4], int tb, R thr2, typename C2<R>::T thr_pivot,
+                                           DiagShared<R>& sh, int32_t* __restrict__ pert) {
+    using T = typename C2<R>::T;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    for (int cl = 0; cl < 16; ++cl) {
+        const int c = 16 * JC + cl;
+        if (c >= tb) return;   // uniform
+        unsigned long long best = 0;
+#pragma unroll
+        for (int q = 0; q < kDiagThreads / 32; ++q) best = sh.cand[q] > best ? sh.cand[q] : best;
+        const int p = 63 - (int)(best & 0xffffffffu);
+        // (S)
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (ty + 16 * i == p) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) sh.prow[tx + 16 * j] = a[i][j];
+                if (tx == cl) {
+                    const T v = a[i][JC];
+                    const bool small = !(v.x * v.x + v.y * v.y > thr2);   // also catches a zero pivot
+                    sh.inv = crecip(small ? thr_pivot : v);
+                    if (small) atomicAdd(pert, 1);
+                }
+            }
+        if (ty == cl && p != c) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) sh.orow[tx + 16 * j] = a[JC][j];
+        }
+        if (tx == cl) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = ty + 16 * i;
+                sh.colc[(r == p || r == c) ? (r ^ p ^ c) : r] = a[i][JC];
+            }
+        }
+        if (tid == 0) sh.piv[c] = p;
+        __syncthreads();
+        // (U)
+        const T inv = sh.inv;
+        T rj[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) rj[j] = cmul(sh.prow[tx + 16 * j], inv);
+        if (p != c) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (ty + 16 * i == p) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) a[i][j] = sh.orow[tx + 16 * j];
+                }
+        }
+        if (tx == cl) {   // after the swap: column c -> 0, its multiplier -> 1 / pivot
+            rj[JC] = inv;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i][JC] = mk((R)0, (R)0);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const T cr = sh.colc[ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const T t = cmul(cr, rj[j]);
+                a[i][j].x -= t.x;
+                a[i][j].y -= t.y;
+            }
+        }
+        if (ty == cl) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) a[JC][j] = rj[j];
+        }
+        if (c + 1 < tb) {
+            if (cl < 15) diag_candidates<JC, R>(a, c + 1, c, tb, sh);
+            else if (JC < 3) diag_candidates<(JC < 3 ? JC + 1 : 3), R>(a, c + 1, c, tb, sh);
+        }
+        __syncthreads();
+    }
+}
+
 template <typename R>
-__global__ void __launch_bounds__(kDiagThreads) k_gj_diag(int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
+__global__ void __launch_bounds__(kDiagThreads, 1) k_gj_diag(int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
                                                          int64_t totD, int64_t offD, typename C2<R>::T* __restrict__ pinv,
                                                          R rel_thr, int32_t* __restrict__ perturbed) {
     using T = typename C2<R>::T;
-    __shared__ T prow[kTile], orow[kTile], colc[kTile];
-    __shared__ R cand_m[16];
-    __shared__ int cand_i[16];
-    __shared__ int piv[kTile], perm[kTile], iperm[kTile];
-    __shared__ R s_red[kDiagThreads / 32];
+    __shared__ DiagShared<R> sh;
     const int64_t f = blockIdx.z;
     T* M = Sinv + f * totD + offD;
     const int64_t k0 = (int64_t)k * kTile;
@@ -251,110 +374,26 @@ __global__ void __launch_bounds__(kDiagThreads) k_gj_diag(int64_t w, int k, type
         }
 #pragma unroll
     for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if (lane == 0) s_red[wid] = mx;
-    if (tx == 0) {   // candidates of column 0
-        R bm = -1;
-        int bi = kTile;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int r = ty + 16 * i;
-            const R m2 = a[i][0].x * a[i][0].x + a[i][0].y * a[i][0].y;
-            if (r < tb && m2 > bm) { bm = m2; bi = r; }
-        }
-        cand_m[ty] = bm;
-        cand_i[ty] = bi;
-    }
+    if (lane == 0) sh.red[wid] = mx;
+    diag_candidates<0, R>(a, 0, -1, tb, sh);
     __syncthreads();
     R thr2 = 0;
 #pragma unroll
-    for (int i = 0; i < kDiagThreads / 32; ++i) thr2 = max(thr2, s_red[i]);
+    for (int i = 0; i < kDiagThreads / 32; ++i) thr2 = max(thr2, sh.red[i]);
     thr2 *= rel_thr * rel_thr;   // |pivot|^2 at or below this is replaced
-    for (int c = 0; c < tb; ++c) {
-        R best = cand_m[0];
-        int p = cand_i[0];
-#pragma unroll
-        for (int i = 1; i < 16; ++i) {
-            const R m2 = cand_m[i];
-            const int ii = cand_i[i];
-            if (m2 > best || (m2 == best && ii < p)) { best = m2; p = ii; }
-        }
-        const bool small = !(best > thr2);   // also catches a zero column
-        if (p >= tb) p = c;
-        // (S) row p, row c and column c into shared memory
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int r = ty + 16 * i;
-            if (r == p) {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) prow[tx + 16 * j] = a[i][j];
-            }
-            if (r == c && p != c) {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) orow[tx + 16 * j] = a[i][j];
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (tx + 16 * j == c) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i) colc[ty + 16 * i] = a[i][j];
-            }
-        if (tid == 0) {
-            piv[c] = p;
-            if (small) atomicAdd(perturbed + f, 1);
-        }
-        __syncthreads();
-        // (U) rank-1 update; row c becomes the scaled pivot row, row p the old row c
-        const T pv = small ? mk(thr2 > 0 ? (R)sqrt(thr2) : (R)1, (R)0) : prow[c];
-        const T inv = crecip(pv);
-        T rj[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) rj[j] = cmul(prow[tx + 16 * j], inv);
-        const int cn = c + 1;
-        R bm = -1;
-        int bi = kTile;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int r = ty + 16 * i;
-            if (r == c) {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) a[i][j] = (tx + 16 * j == c) ? inv : rj[j];
-            } else {
-                const bool isp = r == p;
-                const T cr = isp ? colc[c] : colc[r];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int cc = tx + 16 * j;
-                    T v = isp ? orow[cc] : a[i][j];
-                    if (cc == c) {
-                        const T t = cmul(cr, inv);
-                        v = mk(-t.x, -t.y);
-                    } else {
-                        const T t = cmul(cr, rj[j]);
-                        v.x -= t.x;
-                        v.y -= t.y;
-                    }
-                    a[i][j] = v;
-                    if (cc == cn && r > c && r < tb) {
-                        const R m2 = v.x * v.x + v.y * v.y;
-                        if (m2 > bm) { bm = m2; bi = r; }
-                    }
-                }
-            }
-        }
-        if (tx == (cn & 15)) {
-            cand_m[ty] = bm;
-            cand_i[ty] = bi;
-        }
-        __syncthreads();
-    }
+    const T thr_pivot = mk(thr2 > 0 ? (R)sqrt(thr2) : (R)1, (R)0);
+    int32_t* pert = perturbed + f;
+    diag_block<0, R>(a, tb, thr2, thr_pivot, sh, pert);
+    diag_block<1, R>(a, tb, thr2, thr_pivot, sh, pert);
+    diag_block<2, R>(a, tb, thr2, thr_pivot, sh, pert);
+    diag_block<3, R>(a, tb, thr2, thr_pivot, sh, pert);
     if (tid == 0) {   // the swaps in reverse give the column permutation; iperm is its inverse
-        for (int c = 0; c < kTile; ++c) perm[c] = c;
+        for (int c = 0; c < kTile; ++c) sh.perm[c] = c;
         for (int c = tb - 1; c >= 0; --c) {
-            const int q = piv[c];
-            if (q != c) { const int t = perm[c]; perm[c] = perm[q]; perm[q] = t; }
+            const int q = sh.piv[c];
+            if (q != c) { const int t = sh.perm[c]; sh.perm[c] = sh.perm[q]; sh.perm[q] = t; }
         }
-        for (int c = 0; c < kTile; ++c) iperm[perm[c]] = c;
+        for (int c = 0; c < kTile; ++c) sh.iperm[sh.perm[c]] = c;
     }
     __syncthreads();
     // column cc of the unpermuted inverse is column iperm[cc] of the result
@@ -365,7 +404,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_gj_diag(int64_t w, int k, type
         for (int j = 0; j < 4; ++j) {
             const int r = ty + 16 * i, cc = tx + 16 * j;
             if (r < tb && cc < tb) {
-                const int cd = iperm[cc];
+                const int cd = sh.iperm[cc];
                 M[(k0 + r) * w + k0 + cd] = a[i][j];
                 P[r * kTile + cd] = a[i][j];
             }
@@ -374,10 +413,13 @@ __global__ void __launch_bounds__(kDiagThreads) k_gj_diag(int64_t w, int k, type
 
 // mode 0: row panel  M[k, c] = Pinv M[k, c]       (grid: column tiles x 1 x F, c != k)
 // mode 1: col panel  M[r, k] = -M[r, k] Pinv      (grid: row tiles x 1 x F, r != k)
-// mode 2: update     M[r, c] -= M[r, k] M[k, c]   (grid: column tiles x row tiles x F, r, c != k)
+// mode 2: update     M[r, c] -= M[r, k] M[k, c]   (grid: column tiles x row tiles x F, r, c != k),
+//         skipping tile (la, la) when la >= 0
+// mode 3: the update of tile (la, la) alone       (grid: 1 x 1 x F)
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_gj_panel(int mode, int64_t w, int k, typename C2<R>::T* __restrict__ Sinv,
-                                                       int64_t totD, int64_t offD, const typename C2<R>::T* __restrict__ pinv) {
+                                                       int64_t totD, int64_t offD, const typename C2<R>::T* __restrict__ pinv,
+                                                       int la) {
     using T = typename C2<R>::T;
     __shared__ Tile<R> sm;
     const int64_t f = blockIdx.z;
@@ -409,9 +451,10 @@ __global__ void __launch_bounds__(kThreads) k_gj_panel(int mode, int64_t w, int 
         out = M + r0 * w + k0;
         tile_mac<R>(acc, out, w, P, kTile, nr, nc, tb, sm);
     } else {
-        if ((int)blockIdx.x == k || (int)blockIdx.y == k) return;
-        r0 = (int64_t)blockIdx.y * kTile;
-        c0 = (int64_t)blockIdx.x * kTile;
+        const int bx = mode == 3 ? la : (int)blockIdx.x, by = mode == 3 ? la : (int)blockIdx.y;
+        if (bx == k || by == k || (mode == 2 && bx == la && by == la)) return;
+        r0 = (int64_t)by * kTile;
+        c0 = (int64_t)bx * kTile;
         nr = (int)min((int64_t)kTile, w - r0);
         nc = (int)min((int64_t)kTile, w - c0);
         out = M + r0 * w + c0;
@@ -726,6 +769,7 @@ struct emg_slab {
     int32_t* kcnt = nullptr;          // per-tile arrival counters (zero between launches)
     int64_t kcnt_n = 0;
     int use_tc = 0;                   // wide-group products of FP32 factors on the tcgen05 tensor cores
+    int tc_factor = 1;                // rank-64 updates of FP32 factorizations on the tcgen05 tensor cores
     int wide = 8;                     // column groups at least this wide use the tiled products
     int max_splits = 8;               // split-K cap of the tiled products
     int32_t* tc_status = nullptr;     // set by a tensor-core tile whose bounded wait ran out
@@ -964,7 +1008,8 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
     if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->Cval), F * std::max<int64_t>(s->nC, 1), "slab C values");
     if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->Uval), F * std::max<int64_t>(s->nU, 1), "slab U values");
     if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->UCval), F * std::max<int64_t>(s->nU, 1), "slab U values (by column)");
-    if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->pinv), F * kTile * kTile, "slab pivot tiles");
+    // two sets of pivot-tile inverses: step k's is read while step k + 1's is formed
+    if (!rc) rc = dalloc(reinterpret_cast<T**>(&s->pinv), 2 * F * kTile * kTile, "slab pivot tiles");
     if (!rc) rc = dalloc(&s->perturbed, 2 * F, "slab pivot counters");
     if (rc) { slab_free_factors(s); return rc; }
     s->F = F;
@@ -1001,6 +1046,28 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
     EMG_CUDA(cudaGetLastError());
     EMG_CUDA(cudaFuncSetAttribute(k_schur<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSchurSmem));
     const R rel_thr = sizeof(R) == 4 ? (R)1e-6 : (R)1e-13;
+    // the side stream of the pivot-tile lookahead and its two events
+    struct Side {
+        cudaStream_t st = nullptr;
+        cudaEvent_t tile_ready = nullptr, diag_done = nullptr;
+        ~Side() {
+            if (tile_ready) cudaEventDestroy(tile_ready);
+            if (diag_done) cudaEventDestroy(diag_done);
+            if (st) cudaStreamDestroy(st);
+        }
+    } side;
+    // the pivot-tile inverses are on the critical path: the side stream gets the highest priority
+    int prio_lo = 0, prio_hi = 0;
+    EMG_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    EMG_CUDA(cudaStreamCreateWithPriority(&side.st, cudaStreamNonBlocking, prio_hi));
+    const bool tc_update = sizeof(R) == 4 && s->tc_factor;
+    if (tc_update && !s->tc_status) {
+        rc = dalloc(&s->tc_status, 1, "slab tensor-core status");
+        if (rc) return rc;
+        EMG_CUDA(cudaMemsetAsync(s->tc_status, 0, sizeof(int32_t), st));
+    }
+    EMG_CUDA(cudaEventCreateWithFlags(&side.tile_ready, cudaEventDisableTiming));
+    EMG_CUDA(cudaEventCreateWithFlags(&side.diag_done, cudaEventDisableTiming));
     for (int i = 0; i < s->m; ++i) {
         const int64_t w = s->off[i + 1] - s->off[i];
         if (i > 0) {
@@ -1018,15 +1085,35 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
         if (refine > 0)   // keep S_i for the refinement
             EMG_CUDA(cudaMemcpy2DAsync(Scopy, sizeof(T) * sq, Sinv + s->offD[i], sizeof(T) * s->totD, sizeof(T) * w * w,
                                        (size_t)F, cudaMemcpyDeviceToDevice, st));
+        // Block Gauss-Jordan over the tile steps with a one-step lookahead: the pivot tile
+        // of step k + 1 is updated first and inverted on the side stream while the rest
+        // of step k's update and its column panel run on st.  Step k + 1 waits for it.
+        T* const P0 = static_cast<T*>(s->pinv);
+        auto pset = [&](int k) { return P0 + (int64_t)(k & 1) * F * kTile * kTile; };
+        k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kDiagThreads, 0, st>>>(w, 0, Sinv, s->totD, s->offD[i], pset(0),
+                                                                  rel_thr, s->perturbed);
         for (int k = 0; k < nt; ++k) {
-            k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kDiagThreads, 0, st>>>(w, k, Sinv, s->totD, s->offD[i],
-                                                                      static_cast<T*>(s->pinv), rel_thr, s->perturbed);
-            if (nt > 1) {
-                const T* P = static_cast<const T*>(s->pinv);
-                k_gj_panel<R><<<dim3(nt, 1, (unsigned)F), kThreads, 0, st>>>(0, w, k, Sinv, s->totD, s->offD[i], P);
-                k_gj_panel<R><<<dim3(nt, nt, (unsigned)F), kThreads, 0, st>>>(2, w, k, Sinv, s->totD, s->offD[i], P);
-                k_gj_panel<R><<<dim3(nt, 1, (unsigned)F), kThreads, 0, st>>>(1, w, k, Sinv, s->totD, s->offD[i], P);
+            if (k > 0) EMG_CUDA(cudaStreamWaitEvent(st, side.diag_done, 0));
+            if (nt == 1) break;
+            const T* P = pset(k);
+            const int la = k + 1 < nt ? k + 1 : -1;
+            k_gj_panel<R><<<dim3(nt, 1, (unsigned)F), kThreads, 0, st>>>(0, w, k, Sinv, s->totD, s->offD[i], P, -1);
+            if (la >= 0) {
+                k_gj_panel<R><<<dim3(1, 1, (unsigned)F), kThreads, 0, st>>>(3, w, k, Sinv, s->totD, s->offD[i], P, la);
+                EMG_CUDA(cudaEventRecord(side.tile_ready, st));
+                EMG_CUDA(cudaStreamWaitEvent(side.st, side.tile_ready, 0));
+                k_gj_diag<R><<<dim3(1, 1, (unsigned)F), kDiagThreads, 0, side.st>>>(w, la, Sinv, s->totD, s->offD[i],
+                                                                               pset(la), rel_thr, s->perturbed);
+                EMG_CUDA(cudaEventRecord(side.diag_done, side.st));
             }
+            if (tc_update)
+                rc = emg::tc_gj_update(w, k, la, F, reinterpret_cast<float2*>(Sinv), s->totD, s->offD[i],
+                                       s->tc_status, st);
+            else
+                k_gj_panel<R><<<dim3(nt, nt, (unsigned)F), kThreads, 0, st>>>(2, w, k, Sinv, s->totD, s->offD[i], P,
+                                                                               la);
+            if (rc) return rc;
+            k_gj_panel<R><<<dim3(nt, 1, (unsigned)F), kThreads, 0, st>>>(1, w, k, Sinv, s->totD, s->offD[i], P, -1);
         }
         // X <- X (2I - S X): squares the residual I - S X of the inverse.  S_i's copy
         // is free once 2I - S X is formed and receives the new X.
@@ -1042,8 +1129,16 @@ int slab_factor_t(emg_slab* s, int64_t F, const int32_t* amat_h, int64_t Bm, con
         EMG_CUDA(cudaGetLastError());
     }
     std::vector<int32_t> pc(2 * F);
+    int32_t tcs = 0;
     EMG_CUDA(cudaMemcpyAsync(pc.data(), s->perturbed, sizeof(int32_t) * 2 * F, cudaMemcpyDeviceToHost, st));
+    if (tc_update) EMG_CUDA(cudaMemcpyAsync(&tcs, s->tc_status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     EMG_CUDA(cudaStreamSynchronize(st));
+    if (tcs) {   // a tensor-core tile gave up waiting: the factors are not usable
+        EMG_CUDA(cudaMemset(s->tc_status, 0, sizeof(int32_t)));
+        slab_free_factors(s);
+        set_error("slab factor: a tensor-core update tile timed out waiting for its MMAs");
+        return EMG_ERR_CUDA;
+    }
     s->n_perturbed = 0;
     s->n_refine_skipped = 0;
     for (int64_t f = 0; f < F; ++f) {
@@ -1255,6 +1350,12 @@ extern "C" int emg_gmres_slab(const emg_rplan* pc, emg_slab* s, int64_t Bc, cons
     const int rc = gmres_run(p, Bc, Am, reinterpret_cast<const double2*>(rhs), reinterpret_cast<double2*>(x), restart,
                              max_iter, tol, iters_out, resid_out, (cudaStream_t)stream, M, true);
     return rc ? rc : tc_check(s, (cudaStream_t)stream);
+}
+
+extern "C" int emg_slab_set_factor_tensor_cores(emg_slab* s, int on) {
+    EMG_CHECK_ARG(s, "emg_slab_set_factor_tensor_cores: NULL argument");
+    s->tc_factor = on ? 1 : 0;
+    return EMG_OK;
 }
 
 extern "C" int emg_slab_set_tensor_cores(emg_slab* s, int on) {

@@ -350,6 +350,242 @@ __global__ void __launch_bounds__(kThreads) k_cgemm_tf32(int64_t w, int64_t row0
                      : "memory");
 }
 
+// Rank-64 update of the block Gauss-Jordan inversion on the tensor cores, in
+// FP32-equivalent precision: M[r, c] -= M[r, K] M[K, c] over a 128-row x 64-column
+// block of the w x w complex64 matrix M (row-major, interleaved), K = the 64 columns /
+// rows of pivot tile k.  Each operand x is split as hi = tf32(x) and lo = x - hi, and
+// the product is accumulated from hi*hi + hi*lo + lo*hi (the lo*lo term is below FP32
+// rounding), i.e. 12 MMAs (M = 128, N = 64, K = 8) per K step of 8 for the four real
+// products of the complex one: the real accumulator (TMEM columns 0-63) takes
+// Re*Re - Im*Im (negation in the instruction descriptor), the imaginary one (columns
+// 64-127) Re*Im + Im*Re.
+// One CTA of 256 threads per SM:
+//   1. every thread loads its share of both operands (all 64 K) into registers, so
+//      the whole block's loads are in flight at once;
+//   2. they are split and stored as two 32-wide K chunks (192 KB of shared memory in
+//      the canonical K-major layout; a half-warp stores one 8 x 4 core matrix);
+//   3. one thread issues the 96 MMAs; meanwhile every thread loads its part of the
+//      output block (coalesced rows);
+//   4. the accumulators go TMEM -> shared memory, and the output block is written
+//      back minus the product.
+// Rows of tile k, and tile (la, la) when la >= 0, keep their values.  Grid: column
+// tiles x row blocks of 128 x F (column tile k returns at once).
+constexpr int kUpdM = 128, kUpdN = 64, kUpdTile = 64, kUpdThreads = 256;
+constexpr int kUpdATile = kUpdM * kK * 4;                  // one 128 x 32 FP32 tile: 16 KB
+constexpr int kUpdBTile = kUpdN * kK * 4;                  // one 64 x 32 FP32 tile: 8 KB
+constexpr int kUpdChunk = 4 * kUpdATile + 4 * kUpdBTile;   // one K chunk: 96 KB
+constexpr int kUpdSmem = 2 * kUpdChunk;                    // the epilogue reuses 66.5 KB of it
+constexpr int kUpdLd = kUpdN + 1;                          // row stride of the staged product (float2)
+
+__device__ __forceinline__ float tf32_hi(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__global__ void __launch_bounds__(kUpdThreads, 1) k_gj_update_tc(int64_t w, int k, int la, float2* __restrict__ Sinv,
+                                                                  int64_t totD, int64_t offD,
+                                                                  int32_t* __restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char dsm[];
+    char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(dsm) + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_fail;
+    const int cx = (int)blockIdx.x;
+    if (cx == k) return;               // uniform per CTA, before any TMEM allocation
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float2* M = Sinv + (int64_t)blockIdx.z * totD + offD;
+    const int64_t r0 = (int64_t)blockIdx.y * kUpdM, c0 = (int64_t)cx * kUpdN, k0 = (int64_t)k * kUpdTile;
+    const int tb = (int)min((int64_t)kUpdTile, w - k0);
+    const float2 z2 = make_float2(0.f, 0.f);
+    if (tid == 0) {
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(2 * kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // 1. operand loads.  A: warp item wi = warp + 8 it (it < 16) is row block wi / 8 and
+    //    8-wide K block wi % 8; lane -> row (lane & 15) >> 1, K pair 2 (lane & 1) + 4 (lane >> 4).
+    //    B: item wi = warp + 8 it (it < 8) is 16-wide column block wi / 16 and 4-deep K
+    //    block wi % 16; lane -> column pair 2 (lane & 3) + 8 (lane >> 4), K (lane >> 2) & 3.
+    const int ar = (lane & 15) >> 1, aq = ((lane & 1) << 1) + ((lane >> 4) << 2);
+    const int bp = ((lane & 3) << 1) + ((lane >> 4) << 3), bk = (lane >> 2) & 3;
+    float2 va[16][2], vb[8][2];
+#pragma unroll
+    for (int it = 0; it < 16; ++it) {
+        const int wi = warp + 8 * it;
+        const int64_t gr = r0 + (wi >> 3) * 8 + ar;
+        const int kk = (wi & 7) * 8 + aq;
+        const float2* src = M + gr * w + k0 + kk;
+        va[it][0] = (gr < w && kk < tb) ? src[0] : z2;
+        va[it][1] = (gr < w && kk + 1 < tb) ? src[1] : z2;
+    }
+#pragma unroll
+    for (int it = 0; it < 8; ++it) {
+        const int wi = warp + 8 * it;
+        const int kk = (wi & 15) * 4 + bk;
+        const int64_t gc = c0 + (wi >> 4) * 16 + bp;
+        const float2* src = M + (k0 + kk) * w + gc;
+        vb[it][0] = (kk < tb && gc < w) ? src[0] : z2;
+        vb[it][1] = (kk < tb && gc + 1 < w) ? src[1] : z2;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = tmem_base;
+    const uint32_t mb = smem_u32(&mbar);
+    // 2. split and store: chunk kk / 32, tiles re hi, re lo, im hi, im lo (A then B)
+#pragma unroll
+    for (int it = 0; it < 16; ++it) {
+        const int wi = warp + 8 * it;
+        const int kk = (wi & 7) * 8 + aq, kc = kk & 31;
+        char* cb = base + (kk >> 5) * kUpdChunk;
+        const uint32_t o = (uint32_t)((((wi >> 3) * (kK / 4) + (kc >> 2)) * 128) + ar * 16 + (kc & 3) * 4);
+        const float2 x0 = va[it][0], x1 = va[it][1];
+        const float r0h = tf32_hi(x0.x), r1h = tf32_hi(x1.x), i0h = tf32_hi(x0.y), i1h = tf32_hi(x1.y);
+        *reinterpret_cast<float2*>(cb + 0 * kUpdATile + o) = make_float2(r0h, r1h);
+        *reinterpret_cast<float2*>(cb + 1 * kUpdATile + o) = make_float2(x0.x - r0h, x1.x - r1h);
+        *reinterpret_cast<float2*>(cb + 2 * kUpdATile + o) = make_float2(i0h, i1h);
+        *reinterpret_cast<float2*>(cb + 3 * kUpdATile + o) = make_float2(x0.y - i0h, x1.y - i1h);
+    }
+#pragma unroll
+    for (int it = 0; it < 8; ++it) {
+        const int wi = warp + 8 * it;
+        const int kk = (wi & 15) * 4 + bk, kc = kk & 31;
+        char* cb = base + (kk >> 5) * kUpdChunk + 4 * kUpdATile;
+        const int n = (wi >> 4) * 16 + bp;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int ne = n + e;
+            const uint32_t o = (uint32_t)((((ne >> 3) * (kK / 4) + (kc >> 2)) * 128) + (ne & 7) * 16 + (kc & 3) * 4);
+            const float2 x = vb[it][e];
+            const float rh = tf32_hi(x.x), ih = tf32_hi(x.y);
+            *reinterpret_cast<float*>(cb + 0 * kUpdBTile + o) = rh;
+            *reinterpret_cast<float*>(cb + 1 * kUpdBTile + o) = x.x - rh;
+            *reinterpret_cast<float*>(cb + 2 * kUpdBTile + o) = ih;
+            *reinterpret_cast<float*>(cb + 3 * kUpdBTile + o) = x.y - ih;
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // 3. the MMAs (one thread), then every thread loads its part of the output block:
+    //    element (idx / 64, idx % 64), idx = tid + 256 q
+    if (tid == 0) {
+        const uint32_t id = idesc_tf32(kUpdM, kUpdN), idneg = id | (1u << 13);
+        const uint32_t dre = taddr, dim = taddr + kTmemCols;
+#pragma unroll
+        for (int ch = 0; ch < 2; ++ch) {
+            const uint32_t a0 = smem_u32(base + ch * kUpdChunk), b0 = a0 + 4 * kUpdATile;
+#pragma unroll
+            for (int ks = 0; ks < kK / 8; ++ks) {
+                const uint32_t off = ks * 256;
+                const uint64_t arh = make_desc(a0 + 0 * kUpdATile + off, 128, 1024);
+                const uint64_t arl = make_desc(a0 + 1 * kUpdATile + off, 128, 1024);
+                const uint64_t aih = make_desc(a0 + 2 * kUpdATile + off, 128, 1024);
+                const uint64_t ail = make_desc(a0 + 3 * kUpdATile + off, 128, 1024);
+                const uint64_t brh = make_desc(b0 + 0 * kUpdBTile + off, 128, 1024);
+                const uint64_t brl = make_desc(b0 + 1 * kUpdBTile + off, 128, 1024);
+                const uint64_t bih = make_desc(b0 + 2 * kUpdBTile + off, 128, 1024);
+                const uint64_t bil = make_desc(b0 + 3 * kUpdBTile + off, 128, 1024);
+                const uint32_t first = (ch == 0 && ks == 0) ? 0u : 1u;
+#define EMG_UMMA(D, A, B, ID, ACC)                                                              \
+    asm volatile(                                                                               \
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"                                       \
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(D), "l"(A), "l"(B), \
+        "r"(ID), "r"(ACC)                                                                       \
+        : "memory")
+                EMG_UMMA(dre, arh, brh, id, first);
+                EMG_UMMA(dre, arh, brl, id, 1u);
+                EMG_UMMA(dre, arl, brh, id, 1u);
+                EMG_UMMA(dre, aih, bih, idneg, 1u);
+                EMG_UMMA(dre, aih, bil, idneg, 1u);
+                EMG_UMMA(dre, ail, bih, idneg, 1u);
+                EMG_UMMA(dim, arh, bih, id, first);
+                EMG_UMMA(dim, arh, bil, id, 1u);
+                EMG_UMMA(dim, arl, bih, id, 1u);
+                EMG_UMMA(dim, aih, brh, id, 1u);
+                EMG_UMMA(dim, aih, brl, id, 1u);
+                EMG_UMMA(dim, ail, brh, id, 1u);
+#undef EMG_UMMA
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                     : "memory");
+    }
+    constexpr int kQ = kUpdM * kUpdN / kUpdThreads;   // 32 output entries per thread
+    float2 vc[kQ];
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+        const int idx = tid + kUpdThreads * q;
+        const int64_t gr = r0 + idx / kUpdN, gc = c0 + idx % kUpdN;
+        vc[q] = (gr < w && gc < w) ? M[gr * w + gc] : z2;
+    }
+    if (!mbar_wait(mb, 0u)) s_fail = 1;
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // 4. warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows), columns 32 (w / 4) .. + 31
+    if (!s_fail) {
+        float2* P = reinterpret_cast<float2*>(base);
+        const int row = (warp & 3) * 32 + lane, ch0 = (warp >> 2) * 32;
+        const uint32_t lane_addr = taddr + ((uint32_t)((warp & 3) * 32) << 16);
+#pragma unroll
+        for (int cb = 0; cb < 32; cb += 16) {
+            uint32_t vr[16], vi[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(vr[0]), "=r"(vr[1]), "=r"(vr[2]), "=r"(vr[3]), "=r"(vr[4]), "=r"(vr[5]), "=r"(vr[6]),
+                  "=r"(vr[7]), "=r"(vr[8]), "=r"(vr[9]), "=r"(vr[10]), "=r"(vr[11]), "=r"(vr[12]), "=r"(vr[13]),
+                  "=r"(vr[14]), "=r"(vr[15])
+                : "r"(lane_addr + (uint32_t)(ch0 + cb))
+                : "memory");
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(vi[0]), "=r"(vi[1]), "=r"(vi[2]), "=r"(vi[3]), "=r"(vi[4]), "=r"(vi[5]), "=r"(vi[6]),
+                  "=r"(vi[7]), "=r"(vi[8]), "=r"(vi[9]), "=r"(vi[10]), "=r"(vi[11]), "=r"(vi[12]), "=r"(vi[13]),
+                  "=r"(vi[14]), "=r"(vi[15])
+                : "r"(lane_addr + kTmemCols + (uint32_t)(ch0 + cb))
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int c = 0; c < 16; ++c)
+                P[row * kUpdLd + ch0 + cb + c] = make_float2(__uint_as_float(vr[c]), __uint_as_float(vi[c]));
+        }
+    }
+    __syncthreads();
+    if (!s_fail) {
+        const float2* P = reinterpret_cast<const float2*>(base);
+        const int64_t lr0 = (int64_t)la * kUpdTile;                   // rows of tile la
+        const bool lacol = la >= 0 && cx == la;
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) {
+            const int idx = tid + kUpdThreads * q;
+            const int r = idx / kUpdN, c = idx % kUpdN;
+            const int64_t gr = r0 + r, gc = c0 + c;
+            if (gr >= w || gc >= w || (gr >= k0 && gr < k0 + kUpdTile) || (lacol && gr >= lr0 && gr < lr0 + kUpdTile))
+                continue;
+            const float2 d = P[r * kUpdLd + c];
+            M[gr * w + gc] = make_float2(vc[q].x - d.x, vc[q].y - d.y);
+        }
+    } else if (tid == 0) {
+        mbar_wait(mb, 0u);   // one more bounded wait for the committed MMAs before the TMEM goes
+        atomicExch(status, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(2 * kTmemCols)
+                     : "memory");
+}
+
 }  // namespace tc
 }  // namespace emg
 
@@ -366,6 +602,24 @@ int tc_slab_product(int64_t w, int64_t row0, int64_t Bc, const void* groups, int
     const dim3 grid((unsigned)((maxcol + tc::kN - 1) / tc::kN), (unsigned)((w + tc::kM - 1) / tc::kM), (unsigned)G);
     tc::k_cgemm_tf32<<<grid, tc::kThreads, tc::kCxSmem + 1024, st>>>(
         w, row0, Bc, static_cast<const tc::TcGroup*>(groups), Sinv, totD, offD, Y, alpha, beta, Out, status);
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+}  // namespace emg
+
+// Rank-64 Gauss-Jordan update of step k on the tensor cores (declared in emg_krylov.cuh).
+namespace emg {
+int tc_gj_update(int64_t w, int k, int la, int64_t F, float2* Sinv, int64_t totD, int64_t offD, int32_t* status,
+                 cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        EMG_CUDA(cudaFuncSetAttribute(tc::k_gj_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      tc::kUpdSmem + 1024));
+        attr = true;
+    }
+    const dim3 grid((unsigned)((w + tc::kUpdN - 1) / tc::kUpdN), (unsigned)((w + tc::kUpdM - 1) / tc::kUpdM),
+                    (unsigned)F);
+    tc::k_gj_update_tc<<<grid, tc::kUpdThreads, tc::kUpdSmem + 1024, st>>>(w, k, la, Sinv, totD, offD, status);
     EMG_CUDA(cudaGetLastError());
     return EMG_OK;
 }

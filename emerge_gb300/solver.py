@@ -218,6 +218,12 @@ class SlabFactor:
         cores (TF32 products, FP32 accumulation)."""
         _lib.call("emg_slab_set_tensor_cores", self._h, int(bool(on)))
 
+    def set_factor_tensor_cores(self, on: bool = True) -> None:
+        """Run the rank-64 updates of FP32 factorizations on the tcgen05 tensor cores
+        with split-TF32 products (FP32-equivalent rounding; the default), or on the
+        CUDA cores in FP32."""
+        _lib.call("emg_slab_set_factor_tensor_cores", self._h, int(bool(on)))
+
     def set_wide_group(self, min_columns: int) -> None:
         """Column groups of at least ``min_columns`` use the tiled dense products."""
         _lib.call("emg_slab_set_wide_group", self._h, int(min_columns))

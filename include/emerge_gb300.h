@@ -273,6 +273,14 @@ int emg_slab_apply(emg_slab* slab, int64_t Bc, const int32_t* cfac, const double
  * the slab solve is a preconditioner, so the TF32 rounding only adds to the FP32
  * factor's own error.  Default off. */
 int emg_slab_set_tensor_cores(emg_slab* slab, int on);
+/* on != 0 (default): the rank-64 updates of FP32 factorizations (emg_slab_factor,
+ * precision 1) run on the tcgen05 tensor cores with split-TF32 products (hi*hi +
+ * hi*lo + lo*hi of x = hi + lo) and FP32 accumulation, i.e. FP32-equivalent rounding;
+ * off: CUDA-core FP32.  FP64 factorizations always use the FP64 pipes.  A tensor-core
+ * tile whose bounded wait runs out makes emg_slab_factor return EMG_ERR_CUDA with the
+ * factors released.  (Replaces nothing in the reference: part of the GPU solver
+ * behind fem/solver.py's solve slot.) */
+int emg_slab_set_factor_tensor_cores(emg_slab* slab, int on);
 /* Column groups of at least min_columns use 64 x 64 tiled dense products (with
  * split-K), narrower ones a warp per row.  Default 8: the tiled products are faster
  * even for 8-column groups (measured 80 vs 156 ms per solve on the 2 mm iris). */

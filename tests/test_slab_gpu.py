@@ -209,3 +209,30 @@ def test_autotune_picks_a_layout_and_solves_stay_exact(system):
         assert np.linalg.norm(X[:, c] - ref) / np.linalg.norm(ref) <= 1e-9
     slab.set_wide_group(8)
     slab.set_max_splits(8)
+
+
+def test_tensor_core_factor_update_matches_cuda_core_fp32(system):
+    """The split-TF32 tcgen05 rank-64 update gives FP32-equivalent factors: the
+    preconditioned solve is as close to SuperLU as with the CUDA-core FP32 update, and
+    FGMRES needs no more iterations."""
+    torch, sysr, slab, Ks, rhs, vals = system
+    assert slab.info()["max_width"] > 128          # several tile steps per slab
+    B = np.concatenate(rhs, axis=1)
+    Bt = torch.as_tensor(B, device="cuda")
+    ref = [spla.spsolve(Ks[c // 2].tocsc(), B[:, c]) for c in range(4)]
+    cmat = torch.tensor([0, 0, 1, 1], dtype=torch.int32, device="cuda")
+    out = {}
+    for on in (False, True):
+        slab.set_factor_tensor_cores(on)
+        slab.factor(vals, [0, 1], "fp32")
+        X = slab.apply(Bt, [0, 0, 1, 1]).cpu().numpy()
+        err = max(np.linalg.norm(X[:, c] - ref[c]) / np.linalg.norm(ref[c]) for c in range(4))
+        x, its, res = slab.gmres(vals, Bt, cmat, [0, 0, 1, 0], tol=1e-10, restart=40, max_iter=400)
+        assert np.all(res <= 1e-10)
+        out[on] = (X, err, its)
+    slab.set_factor_tensor_cores(True)
+    X0, e0, it0 = out[False]
+    X1, e1, it1 = out[True]
+    assert e1 <= 3 * e0 + 1e-12
+    assert np.max(np.abs(X1 - X0)) <= 10 * e0 * np.max(np.abs(X0))
+    assert np.all(np.asarray(it1) <= np.asarray(it0) + 1)
