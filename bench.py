@@ -469,7 +469,10 @@ def run_sweep(args):
                onto their span as every other point's initial guess, then batched
                FGMRES on those columns to the same FP64 residual tolerance.
       mlp    — the same with the BF16 tensor-core MLP (trained on ``--sweep-mlp-train``
-               points) supplying the initial guesses instead of the projection.
+               points' own basis coefficients) supplying the initial guesses instead of
+               the projection.
+      mlp_minres — the network trained instead on the reduced system's minimal-residual
+               coefficients at 256 frequencies, from the projection's training points.
       cold   — the same anchored batched FGMRES from zero initial guesses.
     max|dS| compares each with plain on the plain points (spread points plus the two
     strongest passband peaks), and with an independent per-point check on 16 points
@@ -523,6 +526,10 @@ def run_sweep(args):
         mlp = sw.run_warm(freqs, n_train=min(args.sweep_mlp_train, nf), solver="anchored",
                           n_anchor=args.sweep_anchors, guess="mlp", mlp_steps=args.sweep_mlp_steps, **kw)
         sw._slab_key = None
+        mlp_mr = sw.run_warm(freqs, n_train=min(args.sweep_train, nf), solver="anchored",
+                             n_anchor=args.sweep_anchors, guess="mlp", mlp_steps=args.sweep_mlp_minres_steps,
+                             mlp_target="minres", **kw)
+        sw._slab_key = None
         cold = sw.run_anchored(freqs, n_anchor=args.sweep_anchors, **kw)
         # the passband peaks of |S21| (resonances, where the sweep is hardest): the largest
         # local maxima of the fast sweep's |S21|
@@ -575,6 +582,16 @@ def run_sweep(args):
                 "iterations_predicted_mean": mlp.info["final_iterations_mean"],
                 "iterations_cold_same_points_mean": float(cold.iterations[pred].mean()),
                 "max_abs_dS_vs_plain": float(np.max(np.abs(mlp.S[idx] - plain.S)))},
+        # the network trained on the reduced system's minimal-residual coefficients at
+        # 256 frequencies, from the projection's 12 training points
+        "mlp_minres": {"pts_per_s": nf / mlp_mr.seconds, "seconds": round(mlp_mr.seconds, 3),
+                       "train_points": int(mlp_mr.info["train_points"]),
+                       "train_seconds": round(mlp_mr.info["train_seconds"], 3),
+                       "mlp_seconds": round(mlp_mr.info["guess_seconds"], 3), "mlp_loss": mlp_mr.info["mlp_loss"],
+                       "final_seconds": round(mlp_mr.info["final_seconds"], 3),
+                       "iterations_predicted_mean": mlp_mr.info["final_iterations_mean"],
+                       "iterations_cold_same_points_mean": float(cold.iterations[mlp_mr.info["final_index"]].mean()),
+                       "max_abs_dS_check": float(np.max(np.abs(mlp_mr.S[chk] - check.S)))},
         "cold": {"pts_per_s": nf / cold.seconds, "seconds": round(cold.seconds, 3),
                  "iterations_mean": float(cold.iterations.mean()), "iterations_max": int(cold.iterations.max()),
                  "max_abs_dS_vs_fast": float(np.max(np.abs(cold.S - fast.S)))},
@@ -771,6 +788,8 @@ def main():
     ap.add_argument("--sweep-restart", type=int, default=40)
     ap.add_argument("--sweep-chunk", type=int, default=0, help="points per batched solve (0: as many as fit ~80 GB)")
     ap.add_argument("--sweep-mlp-steps", type=int, default=300)
+    ap.add_argument("--sweep-mlp-minres-steps", type=int, default=1500,
+                    help="training steps of the network on minimal-residual targets")
     ap.add_argument("--sweep-inner", default="fp64", choices=["fp32", "fp64"],
                     help="precision of the Krylov vectors of the fast sweep (its factors are FP32 either way)")
     ap.add_argument("--sweep-refine", type=int, default=0, help="Newton-Schulz step on the FP32 slab inverses")

@@ -20,11 +20,11 @@ from . import _lib
 N_FOURIER = 6
 
 
-def features(fnorm: np.ndarray, port: np.ndarray, n_ports: int) -> np.ndarray:
-    """[f, sin(k pi f/2), cos(k pi f/2) for k=1..6, one-hot port] for f in [-1, 1]."""
+def features(fnorm: np.ndarray, port: np.ndarray, n_ports: int, n_fourier: int = N_FOURIER) -> np.ndarray:
+    """[f, sin(k pi f/2), cos(k pi f/2) for k=1..n_fourier, one-hot port] for f in [-1, 1]."""
     f = np.asarray(fnorm, dtype=np.float64)
     cols = [f]
-    for k in range(1, N_FOURIER + 1):
+    for k in range(1, n_fourier + 1):
         cols.append(np.sin(k * np.pi * f / 2))
         cols.append(np.cos(k * np.pi * f / 2))
     oh = np.zeros((len(f), n_ports))

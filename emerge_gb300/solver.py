@@ -786,14 +786,12 @@ class FrequencySweep:
             self._parts = (Er, Br, Pr)
         return self._parts
 
-    def project(self, Xs: torch.Tensor, freqs, ports=None) -> torch.Tensor:
-        """Minimal-residual initial guesses in span(Xs) for every (frequency, port) column.
+    def _reduced(self, Xs: torch.Tensor):
+        """Orthonormal basis Q of span(Xs) and the Gram blocks of the reduced system.
 
-        With Z_a = (E, B, P_1, ...) Xs and alpha(k) = (1, -k^2, gamma_1(k), ...),
-        A(k) Xs = sum_a alpha_a Z_a, so the normal equations of
-        min ||A(k) Xs y - b(k)|| only need the small Gram blocks Z_a^H Z_b and
-        Z_a^H u_p, computed once.  Returns X0 (n, nf*np).
-        """
+        With Z_a = (E, B, P_1, ...) Q and alpha(k) = (1, -k^2, gamma_1(k), ...),
+        A(k) Q = sum_a alpha_a Z_a, so min ||A(k) Q y - b(k)|| only needs the small
+        blocks Z_a^H Z_b and Z_a^H u_p, computed once: returns (Q, Gab, Hu)."""
         Q, _ = torch.linalg.qr(Xs)                       # orthonormal basis (n, r)
         Q = Q.contiguous()                               # LAPACK order is column-major
         Er, Br, Pr = self._restricted_parts()
@@ -801,12 +799,15 @@ class FrequencySweep:
         cm = torch.zeros(r, dtype=torch.int32, device=self.device)
         Zs = [self.sys.spmv(Er, Q, cm), self.sys.spmv(Br, Q, cm)] + [self.sys.spmv(Pi, Q, cm) for Pi in Pr]
         Zc = torch.stack(Zs)                              # (na, n, r)
-        na = Zc.shape[0]
         Gab = torch.einsum("ani,bnj->abij", Zc.conj(), Zc)               # (na, na, r, r)
         Hu = torch.einsum("ani,np->api", Zc.conj(), self.u_r)           # (na, np, r)
+        return Q, Gab, Hu
+
+    def _min_res_coeffs(self, Gab, Hu, freqs) -> torch.Tensor:
+        """Coefficients y(f, p) (nf, np, r) of min ||A(k) Q y - b_p(k)|| (normal equations)."""
         freqs = np.asarray(freqs, dtype=float)
         k0, gam, beta = self._coeffs(freqs)
-        nf, npo = len(freqs), len(self.ports)
+        nf, npo, na, r = len(freqs), len(self.ports), Gab.shape[0], Gab.shape[2]
         alpha = np.zeros((nf, na), dtype=np.complex128)
         alpha[:, 0] = 1.0
         alpha[:, 1] = -k0 ** 2
@@ -817,35 +818,59 @@ class FrequencySweep:
         bscale = torch.as_tensor(-2j * beta.T * self.amp[None, :], device=self.device)   # (nf, np)
         h = h * bscale[:, :, None]
         # ridge-free solve; G is Hermitian positive definite on a full-rank basis
-        y = torch.linalg.solve(G[:, None, :, :].expand(nf, npo, r, r), h[..., None])[..., 0]   # (nf, np, r)
-        X0 = Q @ y.reshape(nf * npo, r).T                                 # (n, nf*np)
-        return X0
+        return torch.linalg.solve(G[:, None, :, :].expand(nf, npo, r, r), h[..., None])[..., 0]
 
-    def mlp_guess(self, Xs: torch.Tensor, train_freqs, freqs, steps: int = 1500, seed: int = 0):
+    def project(self, Xs: torch.Tensor, freqs, ports=None) -> torch.Tensor:
+        """Minimal-residual initial guesses in span(Xs) for every (frequency, port)
+        column (the reduced system of ``_reduced``).  Returns X0 (n, nf*np)."""
+        Q, Gab, Hu = self._reduced(Xs)
+        y = self._min_res_coeffs(Gab, Hu, freqs)                          # (nf, np, r)
+        return Q @ y.reshape(-1, Q.shape[1]).T                            # (n, nf*np)
+
+    def mlp_guess(self, Xs: torch.Tensor, train_freqs, freqs, steps: int = 1500, seed: int = 0,
+                  target: str = "solutions", n_dense: int = 256, n_fourier: int | None = None):
         """Initial guesses from the warm-start MLP trained on the converged columns Xs.
 
-        Targets are the coefficients of each training column in the orthonormal basis
-        of span(Xs) (real and imaginary parts, each standardised); the network maps
-        (normalised frequency, port) to them.  Returns (X0, final training loss)."""
+        The network maps (normalised frequency, port) to coefficients in the orthonormal
+        basis Q of span(Xs) (real and imaginary parts, each standardised).  Targets:
+          "solutions": the coefficients of the training columns themselves (the
+                       network interpolates between the training frequencies);
+          "minres":    the minimal-residual coefficients of the reduced system at
+                       ``n_dense`` frequencies spread over the band (offset from the
+                       sweep's own), computed from the same converged columns, so the
+                       network learns the reduced solution between the training
+                       points and the guess approaches the projection's.
+        ``n_fourier``: Fourier features of the frequency (default 6 for "solutions",
+        16 for "minres", whose targets resolve the passband's resonances).
+        Returns (X0, final training loss)."""
         from .mlp import MLP, features
-        Q, _ = torch.linalg.qr(Xs)
-        Q = Q.contiguous()
+        nfo = n_fourier if n_fourier is not None else (16 if target == "minres" else 6)
         npo = len(self.ports)
-        Y = (Q.conj().T @ Xs).T                                           # (nt*np, r) complex
+        f_lo, f_hi = float(np.min(freqs)), float(np.max(freqs))
+        fn = lambda f: 2 * (np.asarray(f, dtype=float) - f_lo) / max(f_hi - f_lo, 1e-30) - 1   # noqa: E731
+        if target == "minres":
+            Q, Gab, Hu = self._reduced(Xs)
+            fd = f_lo + (np.arange(n_dense) + 0.5) * (f_hi - f_lo) / n_dense
+            Y = self._min_res_coeffs(Gab, Hu, fd).reshape(n_dense * npo, -1)   # (nd*np, r)
+            tf = fd
+        elif target == "solutions":
+            Q, _ = torch.linalg.qr(Xs)
+            Q = Q.contiguous()
+            Y = (Q.conj().T @ Xs).T                                       # (nt*np, r) complex
+            tf = np.asarray(train_freqs, dtype=float)
+        else:
+            raise ValueError(f"mlp_guess: unknown target {target!r}")
         T = torch.cat([Y.real, Y.imag], dim=1)
         # each output standardised on its own: the basis coefficients span orders of
         # magnitude, and one common scale would leave the small ones unlearned
         mu = T.mean(dim=0, keepdim=True)
         scale = T.std(dim=0, keepdim=True).clamp_min(1e-30 + 1e-12 * T.abs().max().item())
         T = ((T - mu) / scale).to(torch.float32).contiguous()
-        f_lo, f_hi = float(np.min(freqs)), float(np.max(freqs))
-        fn = lambda f: 2 * (np.asarray(f, dtype=float) - f_lo) / max(f_hi - f_lo, 1e-30) - 1   # noqa: E731
-        tf = np.asarray(train_freqs, dtype=float)
-        xt = features(np.repeat(fn(tf), npo), np.tile(np.arange(npo), len(tf)), npo)
+        xt = features(np.repeat(fn(tf), npo), np.tile(np.arange(npo), len(tf)), npo, nfo)
         fq = np.asarray(freqs, dtype=float)
         net = MLP(xt.shape[1], T.shape[1], max_batch=max(64, len(xt), len(fq) * npo), seed=seed, device=self.device)
         hist = net.fit(torch.as_tensor(xt), T, steps=steps, lr=3e-3)
-        xa = features(np.repeat(fn(fq), npo), np.tile(np.arange(npo), len(fq)), npo)
+        xa = features(np.repeat(fn(fq), npo), np.tile(np.arange(npo), len(fq)), npo, nfo)
         P = net.forward(torch.as_tensor(xa)).to(torch.float64) * scale + mu    # (nf*np, 2r)
         r = Q.shape[1]
         yc = torch.complex(P[:, :r], P[:, r:])
@@ -868,10 +893,12 @@ class FrequencySweep:
 
     def run_warm(self, freqs, n_train: int = 32, tol: float = 1e-10, restart: int = 150, max_iter: int = 20000,
                  chunk: int | None = None, guess: str = "projection", solver: str = "ilu0", n_anchor: int = 4,
-                 precision: str = "fp32", mlp_steps: int = 1500, refine: int = 0, inner: str = "fp64") -> SweepResult:
+                 precision: str = "fp32", mlp_steps: int = 1500, refine: int = 0, inner: str = "fp64",
+                 mlp_target: str = "solutions") -> SweepResult:
         """Batched sweep: solve n_train evenly spread points, build an initial guess for
         every point from their span (``guess`` = "projection": minimal residual;
-        "mlp": the warm-start network; "none": zero), then finish all points with
+        "mlp": the warm-start network, trained on ``mlp_target`` (see mlp_guess);
+        "none": zero), then finish all points with
         batched GMRES.  ``solver``: "ilu0" (batched ILU(0)-GMRES) or "anchored"
         (FGMRES preconditioned by slab factors at n_anchor anchors, see run_anchored)."""
         freqs = np.asarray(freqs, dtype=float)
@@ -892,7 +919,7 @@ class FrequencySweep:
         torch.cuda.synchronize()
         tg = time.perf_counter()
         if guess == "mlp":
-            X0, mlp_loss = self.mlp_guess(first.solutions, freqs[tr], freqs, steps=mlp_steps)
+            X0, mlp_loss = self.mlp_guess(first.solutions, freqs[tr], freqs, steps=mlp_steps, target=mlp_target)
         elif guess == "projection":
             X0 = self.project(first.solutions, freqs)
         else:
