@@ -455,6 +455,16 @@ def sweep_rooflines(sw, freqs, n_anchor: int, chunk: int) -> dict:
             "spmv": sp, "slab_apply": ap}
 
 
+def factor_rate(sl, n_factors: int, seconds: float) -> dict:
+    off, _ = sl.levels()
+    w = np.diff(off).astype(np.float64)
+    flops = 8.0 * float(np.sum(w ** 3)) * n_factors
+    tf = flops / seconds / 1e12 if seconds > 0 else None
+    return {"gj_flops": flops, "achieved_tflops": tf, "fp32_cuda_core_tflops": FP32_TFLOPS,
+            "frac_of_fp32_cuda_core": tf / FP32_TFLOPS if tf else None,
+            "note": "wall time of the whole factorization (pivot-tile chain, panels, Schur complements)"}
+
+
 def run_sweep(args):
     """Iris-filter sweep: batched + mixed-precision + warm-started vs the plain FP64 GPU solve.
 
@@ -474,6 +484,8 @@ def run_sweep(args):
       mlp_minres — the network trained instead on the reduced system's minimal-residual
                coefficients at 256 frequencies, from the projection's training points.
       cold   — the same anchored batched FGMRES from zero initial guesses.
+      plain_fp32_factor — plain with a complex-FP32 factorization per point and FP64
+               FGMRES to the same tolerance (the per-point method without the FP64 rate).
     max|dS| compares each with plain on the plain points (spread points plus the two
     strongest passband peaks), and with an independent per-point check on 16 points
     that include the five passband peaks (``check``).  ``roofline``: the HBM rooflines
@@ -539,6 +551,9 @@ def run_sweep(args):
         # the plain FP64 solver on spread points plus the two strongest peaks
         idx = np.unique(np.concatenate([idx, peaks_i[np.argsort(s21[peaks_i])[::-1][:args.sweep_plain_peaks]]]))
         plain = sw.run(freqs[idx], method="plain", precond="slab64", tol=args.sweep_tol)
+        # the same per-point method with a complex-FP32 factorization and FP64 FGMRES: the
+        # per-point baseline without GB300's FP64 rate in it
+        plain32 = sw.run(freqs[idx], method="plain", precond="slab32", tol=args.sweep_tol)
     # independent check on 16 points (the peaks + spread points): every column
     # preconditioned by a factorization at its own frequency, FGMRES to a 1e-12 FP64
     # residual (no warm start, no shared anchors), untimed
@@ -570,6 +585,9 @@ def run_sweep(args):
         "fast_seconds": round(fast.seconds, 3), "plain_seconds_per_point": round(plain.seconds / len(idx), 3),
         "plain_points_timed": int(len(idx)), "anchors": args.sweep_anchors, "precision_inner": "complex fp32",
         "fast_guess": "projection", "factor_seconds": round(float(fast.info.get("factor_seconds", 0.0)), 3),
+        # Gauss-Jordan flops of the anchors' factorization (8 sum w^3 per factor, complex
+        # multiply-add = 8 flops) over its wall time, against the FP32 CUDA-core rate
+        "factor_rate": factor_rate(sl, args.sweep_anchors, float(fast.info.get("factor_seconds", 0.0))),
         "train_points": int(fast.info["train_points"]), "train_seconds": round(fast.info["train_seconds"], 3),
         "guess_seconds": round(fast.info["guess_seconds"], 3), "final_seconds": round(fast.info["final_seconds"], 3),
         "iterations_fast_mean": float(fast.iterations.mean()), "iterations_fast_max": int(fast.iterations.max()),
@@ -592,6 +610,12 @@ def run_sweep(args):
                        "iterations_predicted_mean": mlp_mr.info["final_iterations_mean"],
                        "iterations_cold_same_points_mean": float(cold.iterations[mlp_mr.info["final_index"]].mean()),
                        "max_abs_dS_check": float(np.max(np.abs(mlp_mr.S[chk] - check.S)))},
+        "plain_fp32_factor": {"pts_per_s": len(idx) / plain32.seconds,
+                              "seconds_per_point": round(plain32.seconds / len(idx), 3),
+                              "iterations_mean": float(plain32.iterations.mean()),
+                              "max_residual": float(plain32.residuals.max()),
+                              "max_abs_dS_vs_plain": float(np.max(np.abs(plain32.S - plain.S))),
+                              "fast_ratio": v_fast / (len(idx) / plain32.seconds)},
         "cold": {"pts_per_s": nf / cold.seconds, "seconds": round(cold.seconds, 3),
                  "iterations_mean": float(cold.iterations.mean()), "iterations_max": int(cold.iterations.max()),
                  "max_abs_dS_vs_fast": float(np.max(np.abs(cold.S - fast.S)))},
@@ -677,9 +701,10 @@ def run_farfield(dev):
 
 
 def run_eigen(args):
-    """Cavity eigenmodes: the smallest ``--eigen`` instances of the seeded 64-cavity batch
-    (sides U[15,40] mm, dielectric cylinder r U[2,6] mm, eps U[2,30], h = 2.2 mm), 10
-    lowest nonzero modes each, one instance after another.  The first instance is
+    """Cavity eigenmodes: ``--eigen`` instances of the seeded 64-cavity batch (sides
+    U[15,40] mm, dielectric cylinder r U[2,6] mm, eps U[2,30], h = 2.2 mm; the smallest,
+    or with ``--eigen-select spread`` instances spread over the size range), 10 lowest
+    nonzero modes each, one instance after another.  The first instance is
     checked against SciPy ARPACK (eigs, shift-invert, the reference's method) on the
     host: max relative eigenvalue error."""
     import scipy.sparse as sps
@@ -689,9 +714,16 @@ def run_eigen(args):
     from emerge_gb300.freq import Assembler
     from emerge_gb300.geometry import cavity_set
     ps = cavity_set(64, seed=4, h=args.eigen_h)
-    order = sorted(range(64), key=lambda i: ps[i].field.n_field)[: args.eigen]
+    by_size = sorted(range(64), key=lambda i: ps[i].field.n_field)
+    if args.eigen_select == "spread":   # evenly spaced size ranks, the smallest and the largest included
+        ranks = np.unique(np.round(np.linspace(0, 63, max(1, args.eigen))).astype(int))
+        order = [by_size[r] for r in ranks]
+        which = f"{len(order)} of 64 seeded PEC cavities at evenly spaced size ranks (smallest to largest)"
+    else:
+        order = by_size[: args.eigen]
+        which = f"{len(order)} smallest of 64 seeded PEC cavities"
     asm = Assembler()
-    out = {"workload": f"{len(order)} smallest of 64 seeded PEC cavities with dielectric cylinders, h={args.eigen_h}",
+    out = {"workload": f"{which} with dielectric cylinders, h={args.eigen_h}",
            "modes": args.eigen_modes, "instances": []}
     total = 0.0
     err = None
@@ -806,6 +838,8 @@ def main():
     ap.add_argument("--eigen-h", type=float, default=2.2e-3)
     ap.add_argument("--eigen-modes", type=int, default=10)
     ap.add_argument("--eigen-check", type=int, default=1, help="ARPACK check of the first instance")
+    ap.add_argument("--eigen-select", default="smallest", choices=["smallest", "spread"],
+                    help="the smallest instances, or instances spread over the size range")
     ap.add_argument("--eigen-only", action="store_true", help="print only the eigen measurement")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
