@@ -725,6 +725,144 @@ __global__ void __launch_bounds__(kThreads) k_slab_gemm(int64_t w, int64_t row0,
         }
 }
 
+// The same product for groups of at most 16 columns (the training and per-point
+// solves): 128 x 16 output tiles, so no work is spent on absent columns.  Thread t
+// owns rows t / 4 and t / 4 + 64 and columns 4 (t % 4) .. + 3 (8 complex
+// accumulators); S^-1 chunks are staged K-major ([k][row]) and Y chunks row-major in
+// shared memory, double-buffered through registers.  K is split over CTAs as in
+// k_slab_gemm (partials reduced by the last split in split order; part slots of
+// kNarrowM x kNarrowN).  Grid: 1 x (row tiles * splits) x groups.
+constexpr int kNarrowM = 128, kNarrowN = 16;
+template <typename R> struct NarrowTile {
+    using T = typename C2<R>::T;
+    static constexpr int BK = sizeof(R) == 4 ? 32 : 16;
+    T s[2][BK][kNarrowM + 1];
+    T y[2][BK][kNarrowN];
+};
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_slab_gemm16(int64_t w, int64_t row0, int64_t Bc,
+                                                          const Group* __restrict__ groups,
+                                                          const typename C2<R>::T* __restrict__ Sinv, int64_t totD,
+                                                          int64_t offD, const typename C2<R>::T* __restrict__ Y, R alpha,
+                                                          int beta, typename C2<R>::T* __restrict__ Out, int splits,
+                                                          typename C2<R>::T* __restrict__ part, int32_t* __restrict__ cnt) {
+    using T = typename C2<R>::T;
+    constexpr int BK = NarrowTile<R>::BK;
+    constexpr int LS = kNarrowM * BK / kThreads;   // S elements per thread and chunk
+    constexpr int LY = BK * kNarrowN / kThreads;   // Y elements per thread and chunk
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NarrowTile<R>& sm = *reinterpret_cast<NarrowTile<R>*>(smem_raw);
+    __shared__ int s_last;
+    const Group g = groups[blockIdx.z];
+    const int rt = (int)blockIdx.y / splits, sp = (int)blockIdx.y % splits;
+    const int64_t r0 = (int64_t)rt * kNarrowM;
+    const int nr = (int)min((int64_t)kNarrowM, w - r0), nc = min(kNarrowN, g.ncol);
+    const int tid = threadIdx.x, ty = tid >> 2, cx = (tid & 3) * 4;
+    const int64_t kper = (w + splits - 1) / splits;
+    const int64_t ks0 = min(w, (int64_t)sp * kper), ks1 = min(w, ks0 + kper);
+    const T* S = Sinv + (int64_t)g.fac * totD + offD + r0 * w;
+    const T* Yb = Y + row0 * Bc + g.col0;
+    T rs[LS], ry[LY];
+    auto load = [&](int64_t k0) {
+#pragma unroll
+        for (int q = 0; q < LS; ++q) {
+            const int idx = tid + kThreads * q;
+            const int r = idx / BK, kk = idx % BK;
+            rs[q] = (r < nr && k0 + kk < ks1) ? S[(int64_t)r * w + k0 + kk] : czero<T>();
+        }
+#pragma unroll
+        for (int q = 0; q < LY; ++q) {
+            const int idx = tid + kThreads * q;
+            const int kk = idx / kNarrowN, c = idx % kNarrowN;
+            ry[q] = (c < nc && k0 + kk < ks1) ? Yb[(k0 + kk) * Bc + c] : czero<T>();
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int q = 0; q < LS; ++q) {
+            const int idx = tid + kThreads * q;
+            sm.s[buf][idx % BK][idx / BK] = rs[q];
+        }
+#pragma unroll
+        for (int q = 0; q < LY; ++q) {
+            const int idx = tid + kThreads * q;
+            sm.y[buf][idx / kNarrowN][idx % kNarrowN] = ry[q];
+        }
+    };
+    T acc[2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
+    if (ks0 < ks1) {
+        load(ks0);
+        store(0);
+        __syncthreads();
+        int buf = 0;
+        for (int64_t k0 = ks0; k0 < ks1; k0 += BK) {
+            const bool more = k0 + BK < ks1;
+            if (more) load(k0 + BK);
+#pragma unroll 8
+            for (int kk = 0; kk < BK; ++kk) {
+                const T a0 = sm.s[buf][kk][ty], a1 = sm.s[buf][kk][ty + 64];
+                T b[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) b[j] = sm.y[buf][kk][cx + j];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    cfma(acc[0][j], a0, b[j]);
+                    cfma(acc[1][j], a1, b[j]);
+                }
+            }
+            if (more) store(buf ^ 1);
+            __syncthreads();
+            buf ^= 1;
+        }
+    }
+    if (splits > 1) {
+        constexpr int kSlot = kNarrowM * kNarrowN;
+        const int64_t tile = (int64_t)blockIdx.z * (gridDim.y / splits) + rt;
+        T* mine = part + (tile * splits + sp) * kSlot;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) mine[(ty + 64 * i) * kNarrowN + cx + j] = acc[i][j];
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) s_last = atomicAdd(cnt + tile, 1) == splits - 1;
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        const T* all = part + tile * splits * kSlot;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int e = (ty + 64 * i) * kNarrowN + cx + j;
+                T v = czero<T>();
+                for (int q = 0; q < splits; ++q) {
+                    const T pq = __ldcg(all + (int64_t)q * kSlot + e);
+                    v.x += pq.x;
+                    v.y += pq.y;
+                }
+                acc[i][j] = v;
+            }
+        if (tid == 0) cnt[tile] = 0;
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = ty + 64 * i, c = cx + j;
+            if (r < nr && c < nc) {
+                T& o = Out[(row0 + r0 + r) * Bc + g.col0 + c];
+                const T res = mk(alpha * acc[i][j].x, alpha * acc[i][j].y);
+                if (beta) { o.x += res.x; o.y += res.y; }
+                else o = res;
+            }
+        }
+}
+
 // K splits of a wide-group product: enough CTAs for two per SM, at least 256
 // columns of K per split, at most max_splits (8 unless tuned).
 inline int gemm_splits(int64_t tiles, int64_t w, int max_splits = 8) {
@@ -1211,13 +1349,17 @@ struct SlabPrecond : emg::Precond {
             const int64_t ct = (maxcol + emg::slab::kTile - 1) / emg::slab::kTile, G = (int64_t)groups.size();
             size_t need = 0;
             int64_t tiles_max = 0;
+            const bool narrow = maxcol <= emg::slab::kNarrowN;
+            const int64_t tm = narrow ? emg::slab::kNarrowM : emg::slab::kTile;
+            const int64_t slot = narrow ? (int64_t)emg::slab::kNarrowM * emg::slab::kNarrowN
+                                        : (int64_t)emg::slab::kTile * emg::slab::kTile;
             for (int i = 0; i < s->m; ++i) {
                 const int64_t w = s->off[i + 1] - s->off[i];
-                const int64_t tiles = ct * ((w + emg::slab::kTile - 1) / emg::slab::kTile) * G;
+                const int64_t tiles = (narrow ? 1 : ct) * ((w + tm - 1) / tm) * G;
                 const int sp = emg::slab::gemm_splits(tiles, w, s->max_splits);
                 tiles_max = std::max(tiles_max, tiles);
                 if (sp > 1)
-                    need = std::max(need, (size_t)tiles * sp * emg::slab::kTile * emg::slab::kTile *
+                    need = std::max(need, (size_t)tiles * sp * (size_t)slot *
                                               (s->prec == 1 ? sizeof(float2) : sizeof(double2)));
             }
             if (need > s->kpart_bytes) {
@@ -1263,7 +1405,14 @@ struct SlabPrecond : emg::Precond {
         const unsigned G = (unsigned)groups.size();
         int maxcol = 0;
         for (const auto& g : groups) maxcol = std::max(maxcol, (int)g.ncol);
-        // dense slab product: warp-per-row for narrow groups, 64 x 64 tiles for wide ones
+        static bool narrow_attr = false;   // per instantiation: the 128 x 16 tiles need 74 KB
+        if (!narrow_attr) {
+            EMG_CUDA(cudaFuncSetAttribute(k_slab_gemm16<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)sizeof(NarrowTile<R>)));
+            narrow_attr = true;
+        }
+        // dense slab product: warp-per-row for groups narrower than s->wide, 128 x 16
+        // tiles up to 16 columns, 64 x 64 tiles for wider ones
         auto dense = [&](int64_t w, int64_t i, R alpha, int beta) {
             if constexpr (sizeof(R) == 4) {
                 if (s->use_tc && maxcol >= s->wide) {
@@ -1274,7 +1423,13 @@ struct SlabPrecond : emg::Precond {
                     return;
                 }
             }
-            if (maxcol >= s->wide) {
+            if (maxcol >= s->wide && maxcol <= kNarrowN) {
+                const int64_t rt = (w + kNarrowM - 1) / kNarrowM;
+                const int sp = gemm_splits(rt * G, w, s->max_splits);
+                k_slab_gemm16<R><<<dim3(1u, (unsigned)(rt * sp), G), kThreads, sizeof(NarrowTile<R>), st>>>(
+                    w, s->off[i], Bc, s->groups, Sinv, s->totD, s->offD[i], Y, alpha, beta, Z, sp,
+                    static_cast<T*>(s->kpart), s->kcnt);
+            } else if (maxcol >= s->wide) {
                 const int64_t ct = (maxcol + kTile - 1) / kTile, rt = (w + kTile - 1) / kTile;
                 const int sp = gemm_splits(ct * rt * G, w, s->max_splits);
                 k_slab_gemm<R><<<dim3((unsigned)ct, (unsigned)(rt * sp), G), kThreads, 0, st>>>(

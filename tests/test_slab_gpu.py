@@ -236,3 +236,22 @@ def test_tensor_core_factor_update_matches_cuda_core_fp32(system):
     assert e1 <= 3 * e0 + 1e-12
     assert np.max(np.abs(X1 - X0)) <= 10 * e0 * np.max(np.abs(X0))
     assert np.all(np.asarray(it1) <= np.asarray(it0) + 1)
+
+
+def test_narrow_tiled_product_matches_row_product_fp32(system):
+    """Groups of 8-16 columns take the 128 x 16 tiled product (split over K); on FP32
+    factors it agrees with the warp-per-row product to FP32 rounding."""
+    torch, sysr, slab, Ks, rhs, vals = system
+    slab.factor(vals, [0, 1], "fp32")
+    rng = np.random.default_rng(7)
+    n = Ks[0].shape[0]
+    B = rng.standard_normal((n, 24)) + 1j * rng.standard_normal((n, 24))
+    Bt = torch.as_tensor(B, device="cuda")
+    cfac = [0] * 12 + [1] * 12
+    tiled = slab.apply(Bt, cfac).cpu().numpy()
+    slab.set_wide_group(1 << 30)
+    try:
+        rows = slab.apply(Bt, cfac).cpu().numpy()
+    finally:
+        slab.set_wide_group(8)
+    assert np.max(np.abs(tiled - rows)) <= 1e-3 * np.max(np.abs(rows))
