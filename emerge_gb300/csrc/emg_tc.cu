@@ -1,6 +1,8 @@
-// 5th-generation tensor-core (tcgen05) TF32 GEMM tile for the dense slab products.
+// 5th-generation tensor-core (tcgen05) kernels: a TF32 GEMM tile, the complex slab
+// product of the slab solve (TF32), and the rank-64 Gauss-Jordan update of FP32 slab
+// factorizations in split-TF32 (FP32-equivalent) precision (k_gj_update_tc, below).
 //
-// D[M x N] = A[M x K] B[N x K]^T (row-major FP32 in and out, TF32 products, FP32
+// GEMM tile: D[M x N] = A[M x K] B[N x K]^T (row-major FP32 in and out, TF32 products, FP32
 // accumulation in tensor memory).  One CTA of 128 threads owns a 128 x 64 tile of D:
 //   - the operands of a 32-wide K chunk are staged by all threads into shared memory
 //     in the canonical K-major, non-swizzled layout (8-row x 16-byte core matrices,
