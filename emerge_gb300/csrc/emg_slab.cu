@@ -24,9 +24,12 @@
 // Gauss-Jordan with 64 x 64 tiles: the pivot tile is inverted by one CTA with
 // partial pivoting inside the tile (a pivot below a relative threshold is replaced
 // by the threshold and counted), the pivot row panel is multiplied by it, every
-// other tile gets a rank-64 update (the bulk of the flops, a tiled complex GEMM),
-// and the pivot column panel is multiplied by minus it.  Several factorizations
-// (anchor frequencies) run in the same launches (grid z), each with its own values.
+// other tile gets a rank-64 update (the bulk of the flops: for FP32 factors on the
+// tcgen05 tensor cores with split-TF32 products, emg_tc.cu; for FP64 a tiled complex
+// GEMM on the FP64 pipes), and the pivot column panel is multiplied by minus it.  The
+// next pivot tile is updated first and inverted on a side stream while the rest of
+// the step runs (one-step lookahead).  Several factorizations (anchor frequencies) run
+// in the same launches (grid z), each with its own values.
 #include <algorithm>
 #include <cmath>
 #include <vector>
