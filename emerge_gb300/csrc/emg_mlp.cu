@@ -1,14 +1,17 @@
-// Small MLP for the sweep warm start: BF16 weights and activations on the tensor
-// cores (mma.sync m16n8k16, FP32 accumulation), FP32 master weights and Adam.
+// Small MLP for the sweep warm start: BF16 weights and activations on the tcgen05
+// tensor cores (kind::f16, FP32 accumulation in tensor memory; emg_tc.cu), FP32 master
+// weights and Adam.
 //
 // The network maps features of (normalised frequency, port) to the coefficients
 // of the sweep's converged-solution basis.  All GEMMs of the forward and the
-// backward pass are one kernel (k_gemm_bf16) with explicit strides:
+// backward pass are one kernel (tc_gemm_bf16) with explicit strides:
 //   forward   Z = H W^T + b         (batch x n) = (batch x k)(k x n)
 //   weights   dW = dZ^T H           (n x k)     = (n x batch)(batch x k)
 //   inputs    dH = dZ W             (batch x k) = (batch x n)(n x k)
-// Each warp computes one 16x8 output tile; the problem sizes (<= 128 x 128 x 256)
-// make this launch-bound, not tensor-bound, so the simple tiling is the right one.
+// The problem sizes (<= a few hundred rows, 128 wide) make it launch-bound, so one
+// 128 x 64 output tile per CTA with unpipelined staging is enough.  A tensor-core wait
+// that runs out sets a sticky status, which the forward and the gradient requests
+// report.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -17,46 +20,12 @@
 #include "emg_common.cuh"
 
 namespace emg {
+// tcgen05 BF16 GEMM (emg_tc.cu): C[m][n] = sum_k A(m,k) B(k,n) (+ bias[n]),
+// A(m,k) = a[m*sam + k*sak], B(k,n) = b[k*sbk + n*sbn]; *status (device) set to 1 if a
+// bounded wait ran out.
+int tc_gemm_bf16(int M, int N, int K, const __nv_bfloat16* a, int sam, int sak, const __nv_bfloat16* b, int sbk,
+                 int sbn, const float* bias, float* C, int ldc, int32_t* status, cudaStream_t st);
 namespace mlp {
-
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
-
-// C[m][n] = sum_k A(m,k) B(k,n) (+ bias[n]); A(m,k) = a[m*sam + k*sak], B(k,n) = b[k*sbk + n*sbn].
-// M % 16 == 0, N % 8 == 0, K % 16 == 0.  mode: 0 = store fp32 C, 1 = store C + bias.
-__global__ void k_gemm_bf16(int M, int N, int K, const __nv_bfloat16* __restrict__ a, int sam, int sak,
-                            const __nv_bfloat16* __restrict__ b, int sbk, int sbn, const float* __restrict__ bias,
-                            float* __restrict__ C, int ldc) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int tiles_n = N / 8;
-    if (warp >= (M / 16) * tiles_n) return;
-    const int m0 = (warp / tiles_n) * 16, n0 = (warp % tiles_n) * 8;
-    const int g = lane >> 2, t = lane & 3;
-    float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
-    for (int k0 = 0; k0 < K; k0 += 16) {
-        auto A = [&](int m, int k) { return a[(size_t)(m0 + m) * sam + (size_t)(k0 + k) * sak]; };
-        auto Bv = [&](int k, int n) { return b[(size_t)(k0 + k) * sbk + (size_t)(n0 + n) * sbn]; };
-        const uint32_t a0 = pack2(A(g, 2 * t), A(g, 2 * t + 1));
-        const uint32_t a1 = pack2(A(g + 8, 2 * t), A(g + 8, 2 * t + 1));
-        const uint32_t a2 = pack2(A(g, 2 * t + 8), A(g, 2 * t + 9));
-        const uint32_t a3 = pack2(A(g + 8, 2 * t + 8), A(g + 8, 2 * t + 9));
-        const uint32_t b0 = pack2(Bv(2 * t, g), Bv(2 * t + 1, g));
-        const uint32_t b1 = pack2(Bv(2 * t + 8, g), Bv(2 * t + 9, g));
-        asm volatile(
-            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-            "{%0,%1,%2,%3};\n"
-            : "+f"(c0), "+f"(c1), "+f"(c2), "+f"(c3)
-            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-    }
-    const int r0 = m0 + g, r1 = m0 + g + 8, cc = n0 + 2 * t;
-    const float bb0 = bias ? bias[cc] : 0.f, bb1 = bias ? bias[cc + 1] : 0.f;
-    C[(size_t)r0 * ldc + cc] = c0 + bb0;
-    C[(size_t)r0 * ldc + cc + 1] = c1 + bb1;
-    C[(size_t)r1 * ldc + cc] = c2 + bb0;
-    C[(size_t)r1 * ldc + cc + 1] = c3 + bb1;
-}
 
 // H = tanh(Z) in bf16 (act = 1) or H = Z in bf16 (act = 0)
 __global__ void k_act(int n, const float* __restrict__ Z, int act, __nv_bfloat16* __restrict__ H) {
@@ -166,6 +135,7 @@ struct emg_mlp {
     float* dH = nullptr;
     float* dZf = nullptr;
     __nv_bfloat16* dZb = nullptr;
+    int32_t* tcstat = nullptr;                           // sticky tensor-core time-out flag
     int step = 0;
 };
 
@@ -177,19 +147,26 @@ void mlp_free(emg_mlp* p) {
     dfree(p->w); dfree(p->g); dfree(p->m1); dfree(p->m2); dfree(p->wb);
     for (auto& h : p->H) dfree(h);
     for (auto& z : p->Z) dfree(z);
-    dfree(p->dYf); dfree(p->dYb); dfree(p->dH); dfree(p->dZf); dfree(p->dZb);
+    dfree(p->dYf); dfree(p->dYb); dfree(p->dH); dfree(p->dZf); dfree(p->dZb); dfree(p->tcstat);
     delete p;
 }
 
 int pad_to(int x, int m) { return (x + m - 1) / m * m; }
 
-int gemm(int M, int N, int K, const __nv_bfloat16* a, int sam, int sak, const __nv_bfloat16* b, int sbk, int sbn,
-         const float* bias, float* C, int ldc, cudaStream_t s) {
-    const int warps = (M / 16) * (N / 8);
-    const int threads = 128;
-    const int blocks = (warps * 32 + threads - 1) / threads;
-    mlp::k_gemm_bf16<<<blocks, threads, 0, s>>>(M, N, K, a, sam, sak, b, sbk, sbn, bias, C, ldc);
-    EMG_CUDA(cudaGetLastError());
+int gemm(emg_mlp* p, int M, int N, int K, const __nv_bfloat16* a, int sam, int sak, const __nv_bfloat16* b, int sbk,
+         int sbn, const float* bias, float* C, int ldc, cudaStream_t s) {
+    return tc_gemm_bf16(M, N, K, a, sam, sak, b, sbk, sbn, bias, C, ldc, p->tcstat, s);
+}
+
+// EMG_ERR_CUDA if a tensor-core GEMM of this network has timed out (the flag stays set)
+int tc_check(emg_mlp* p, cudaStream_t s) {
+    int32_t h = 0;
+    EMG_CUDA(cudaMemcpyAsync(&h, p->tcstat, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    EMG_CUDA(cudaStreamSynchronize(s));
+    if (h) {
+        set_error("mlp: a tensor-core GEMM timed out waiting for its MMAs; the network is not usable");
+        return EMG_ERR_CUDA;
+    }
     return EMG_OK;
 }
 
@@ -197,7 +174,7 @@ int gemm(int M, int N, int K, const __nv_bfloat16* a, int sam, int sak, const __
 int forward(emg_mlp* p, int rows_pad, cudaStream_t s) {
     const int L = (int)p->K.size();
     for (int l = 0; l < L; ++l) {
-        int rc = gemm(rows_pad, p->N[l], p->K[l], p->H[l], p->K[l], 1, p->wb + p->woff[l], 1, p->K[l],
+        int rc = gemm(p, rows_pad, p->N[l], p->K[l], p->H[l], p->K[l], 1, p->wb + p->woff[l], 1, p->K[l],
                       p->w + p->boff[l], p->Z[l], p->N[l], s);
         if (rc) return rc;
         if (l + 1 < L) {
@@ -217,12 +194,12 @@ int backward(emg_mlp* p, int nb, int rows_pad, cudaStream_t s) {
     for (int l = L - 1; l >= 0; --l) {
         const int n = p->N[l], k = p->K[l];
         // dW = dZ^T H : (n x rows)(rows x k)
-        int rc = gemm(n, k, rows_pad, dzb, 1, n, p->H[l], k, 1, nullptr, p->g + p->woff[l], k, s);
+        int rc = gemm(p, n, k, rows_pad, dzb, 1, n, p->H[l], k, 1, nullptr, p->g + p->woff[l], k, s);
         if (rc) return rc;
         mlp::k_bias_grad<<<(n + 127) / 128, 128, 0, s>>>(nb, n, dzf, p->g + p->boff[l]);
         if (l > 0) {
             // dH = dZ W : (rows x n)(n x k)
-            rc = gemm(rows_pad, k, n, dzb, n, 1, p->wb + p->woff[l], k, 1, nullptr, p->dH, k, s);
+            rc = gemm(p, rows_pad, k, n, dzb, n, 1, p->wb + p->woff[l], k, 1, nullptr, p->dH, k, s);
             if (rc) return rc;
             const int e = rows_pad * k;
             mlp::k_act_back<<<(e + 255) / 256, 256, 0, s>>>(e, p->dH, p->Z[l - 1], p->dZb, p->dZf);
@@ -281,6 +258,8 @@ extern "C" int emg_mlp_create(int in_dim, int hidden, int hidden_layers, int out
     if ((rc = dalloc(&p->dH, (int64_t)R * wmax, "mlp dH"))) return fail(rc);
     if ((rc = dalloc(&p->dZf, (int64_t)R * wmax, "mlp dZ"))) return fail(rc);
     if ((rc = dalloc(&p->dZb, (int64_t)R * wmax, "mlp dZ bf16"))) return fail(rc);
+    if ((rc = dalloc(&p->tcstat, 1, "mlp tensor-core status"))) return fail(rc);
+    if (cudaMemset(p->tcstat, 0, sizeof(int32_t)) != cudaSuccess) return fail(cuda_status(cudaGetLastError(), "mlp"));
     // deterministic init: uniform(-1/sqrt(K), 1/sqrt(K)) weights from a splitmix64 stream, zero biases
     std::vector<float> h(off, 0.f);
     uint64_t st = seed;
@@ -338,7 +317,7 @@ extern "C" int emg_mlp_forward(emg_mlp* p, int batch, const float* x, float* y, 
     if (rc) return rc;
     mlp::k_unpad_out<<<(batch * p->out + 255) / 256, 256, 0, s>>>(batch, p->out, p->out_pad, p->Z.back(), y);
     EMG_CUDA(cudaGetLastError());
-    return EMG_OK;
+    return tc_check(p, s);
 }
 
 // One training step (forward, MSE loss, backward; Adam when lr > 0).  grads_out
@@ -356,7 +335,10 @@ extern "C" int emg_mlp_train_step(emg_mlp* p, int batch, const float* x, const f
     mlp::k_loss<<<1, 256, 0, s>>>(batch, p->out, p->out_pad, p->Z.back(), target, p->dYf, p->dYb, loss_out, R);
     rc = backward(p, batch, R, s);
     if (rc) return rc;
-    if (grads_out) EMG_CUDA(cudaMemcpyAsync(grads_out, p->g, sizeof(float) * p->nparam, cudaMemcpyDeviceToDevice, s));
+    if (grads_out) {
+        EMG_CUDA(cudaMemcpyAsync(grads_out, p->g, sizeof(float) * p->nparam, cudaMemcpyDeviceToDevice, s));
+        if ((rc = tc_check(p, s))) return rc;
+    }
     if (lr > 0.f) {
         p->step++;
         const float b1 = 0.9f, b2 = 0.999f;

@@ -16,6 +16,8 @@
 // MMAs it already committed one more bounded wait, skips the remaining work, and still
 // frees its TMEM.  After a nonzero status the host discards the output tile and does
 // not relaunch on the same data.
+#include <cuda_bf16.h>
+
 #include "emg_krylov.cuh"
 
 namespace emg {
@@ -352,6 +354,132 @@ __global__ void __launch_bounds__(kThreads) k_cgemm_tf32(int64_t w, int64_t row0
                      : "memory");
 }
 
+// BF16 GEMM of the warm-start network (tcgen05 kind::f16, FP32 accumulation in TMEM):
+// C[m][n] = sum_k A(m,k) B(k,n) (+ bias[n]) with A(m,k) = a[m sam + k sak] and
+// B(k,n) = b[k sbk + n sbn], so one kernel serves the forward product and both
+// backward products (transposes by strides).  One CTA of 128 threads owns a 128 x 64
+// tile of C: 64-wide K chunks of A and B are staged by all threads into the canonical
+// K-major layout (8-row x 16-byte core matrices, the same byte geometry as the TF32
+// tiles above), one thread issues four MMAs (K = 16 each) per chunk, and every wait is
+// bounded (a time-out sets *status, sticky, and skips the rest of the tile).
+constexpr int kBfK = 64;   // K chunk (128 bytes of BF16 per row)
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ uint32_t bf_off(int r, int k) {   // byte offset of (r, k) in a [rows x 64] tile
+    return (uint32_t)(((r >> 3) * (kBfK / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__global__ void __launch_bounds__(kThreads) k_gemm_bf16_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ a,
+                                                           int sam, int sak, const __nv_bfloat16* __restrict__ b,
+                                                           int sbk, int sbn, const float* __restrict__ bias,
+                                                           float* __restrict__ C, int ldc,
+                                                           int32_t* __restrict__ status) {
+    __shared__ __align__(1024) __nv_bfloat16 sa[kM * kBfK];
+    __shared__ __align__(1024) __nv_bfloat16 sb[kN * kBfK];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * kM, n0 = blockIdx.x * kN;
+    if (tid == 0) {
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = tmem_base;
+    const uint32_t mb = smem_u32(&mbar);
+    const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    uint32_t phase = 0;
+    const int nk = (K + kBfK - 1) / kBfK;
+    for (int kc = 0; kc < nk; ++kc) {
+        const int k0 = kc * kBfK;
+        for (int idx = tid; idx < kM * kBfK; idx += kThreads) {
+            const int r = idx / kBfK, k = idx % kBfK;
+            const int gm = m0 + r, gk = k0 + k;
+            *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(sa) + bf_off(r, k)) =
+                (gm < M && gk < K) ? a[(size_t)gm * sam + (size_t)gk * sak] : zero;
+        }
+        for (int idx = tid; idx < kN * kBfK; idx += kThreads) {
+            const int n = idx / kBfK, k = idx % kBfK;
+            const int gn = n0 + n, gk = k0 + k;
+            *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(sb) + bf_off(n, k)) =
+                (gn < N && gk < K) ? b[(size_t)gk * sbk + (size_t)gn * sbn] : zero;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0 && !s_fail) {
+            const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+            const uint32_t idesc = idesc_bf16(kM, kN);
+#pragma unroll
+            for (int ks = 0; ks < kBfK / 16; ++ks) {
+                // K = 16 BF16 = two core matrices along K: +256 B per step
+                const uint64_t ad = make_desc(a0 + ks * 256, 128, 1024);
+                const uint64_t bd = make_desc(b0 + ks * 256, 128, 1024);
+                const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(taddr),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                         : "memory");
+        }
+        __syncthreads();
+        if (!s_fail) {
+            if (!mbar_wait(mb, phase)) s_fail = 1;
+        }
+        phase ^= 1;
+        __syncthreads();
+        if (s_fail) break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!s_fail) {
+        const uint32_t lane_addr = taddr + ((uint32_t)(warp * 32) << 16);
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll
+        for (int c0 = 0; c0 < kN; c0 += 16) {
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(lane_addr + (uint32_t)c0)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < M) {
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    const int n = n0 + c0 + c;
+                    if (n < N) C[(size_t)row * ldc + n] = __uint_as_float(v[c]) + (bias ? bias[n] : 0.f);
+                }
+            }
+        }
+    } else if (tid == 0) {
+        mbar_wait(mb, phase ^ 1);   // one more bounded wait for the committed MMAs before the TMEM goes
+        atomicExch(status, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kTmemCols) : "memory");
+}
+
 // Rank-64 update of the block Gauss-Jordan inversion on the tensor cores, in
 // FP32-equivalent precision: M[r, c] -= M[r, K] M[K, c] over a 128-row x 64-column
 // block of the w x w complex64 matrix M (row-major, interleaved), K = the 64 columns /
@@ -604,6 +732,17 @@ int tc_slab_product(int64_t w, int64_t row0, int64_t Bc, const void* groups, int
     const dim3 grid((unsigned)((maxcol + tc::kN - 1) / tc::kN), (unsigned)((w + tc::kM - 1) / tc::kM), (unsigned)G);
     tc::k_cgemm_tf32<<<grid, tc::kThreads, tc::kCxSmem + 1024, st>>>(
         w, row0, Bc, static_cast<const tc::TcGroup*>(groups), Sinv, totD, offD, Y, alpha, beta, Out, status);
+    EMG_CUDA(cudaGetLastError());
+    return EMG_OK;
+}
+}  // namespace emg
+
+// BF16 GEMM of the warm-start network on the tensor cores (declared in emg_mlp.cu).
+namespace emg {
+int tc_gemm_bf16(int M, int N, int K, const __nv_bfloat16* a, int sam, int sak, const __nv_bfloat16* b, int sbk,
+                 int sbn, const float* bias, float* C, int ldc, int32_t* status, cudaStream_t st) {
+    const dim3 grid((unsigned)((N + tc::kN - 1) / tc::kN), (unsigned)((M + tc::kM - 1) / tc::kM));
+    tc::k_gemm_bf16_tc<<<grid, tc::kThreads, 0, st>>>(M, N, K, a, sam, sak, b, sbk, sbn, bias, C, ldc, status);
     EMG_CUDA(cudaGetLastError());
     return EMG_OK;
 }

@@ -327,10 +327,12 @@ int emg_tc_gemm_tf32(int64_t M, int64_t N, int64_t K, const float* A, int64_t ld
 /* ------------------------------------------------------ warm-start MLP ---
  * No counterpart in the reference (a sweep acceleration).  A multilayer
  * perceptron in_dim -> hidden_layers x hidden (tanh) -> out_dim with BF16
- * weights and activations, FP32 accumulation on the tensor cores
- * (mma.sync m16n8k16), FP32 master weights and Adam.  Dimensions are padded to
+ * weights and activations, FP32 accumulation on the tcgen05 tensor cores
+ * (kind::f16), FP32 master weights and Adam.  Dimensions are padded to
  * multiples of 16 internally; batches up to max_batch rows.  x, y, target are
- * DEVICE float arrays, row-major (batch x dim). */
+ * DEVICE float arrays, row-major (batch x dim).  A tensor-core wait that runs out
+ * makes emg_mlp_forward (and emg_mlp_train_step with grads_out) return
+ * EMG_ERR_CUDA from then on. */
 typedef struct emg_mlp emg_mlp;
 int emg_mlp_create(int in_dim, int hidden, int hidden_layers, int out_dim, int max_batch, uint64_t seed,
                    emg_mlp** mlp);
