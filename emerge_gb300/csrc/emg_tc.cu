@@ -399,21 +399,45 @@ __global__ void __launch_bounds__(kThreads) k_gemm_bf16_tc(int M, int N, int K, 
     const uint32_t taddr = tmem_base;
     const uint32_t mb = smem_u32(&mbar);
     const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    // operands contiguous along K (16-byte aligned rows, K a multiple of 8) are staged
+    // 8 elements (one core-matrix row) per load; others element by element
+    const bool avec = sak == 1 && sam % 8 == 0 && K % 8 == 0 && (reinterpret_cast<uintptr_t>(a) & 15) == 0;
+    const bool bvec = sbk == 1 && sbn % 8 == 0 && K % 8 == 0 && (reinterpret_cast<uintptr_t>(b) & 15) == 0;
     uint32_t phase = 0;
     const int nk = (K + kBfK - 1) / kBfK;
     for (int kc = 0; kc < nk; ++kc) {
         const int k0 = kc * kBfK;
-        for (int idx = tid; idx < kM * kBfK; idx += kThreads) {
-            const int r = idx / kBfK, k = idx % kBfK;
-            const int gm = m0 + r, gk = k0 + k;
-            *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(sa) + bf_off(r, k)) =
-                (gm < M && gk < K) ? a[(size_t)gm * sam + (size_t)gk * sak] : zero;
+        if (avec) {
+            for (int idx = tid; idx < kM * (kBfK / 8); idx += kThreads) {
+                const int r = idx / (kBfK / 8), k = (idx % (kBfK / 8)) * 8;
+                const int gm = m0 + r, gk = k0 + k;
+                *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sa) + bf_off(r, k)) =
+                    (gm < M && gk < K) ? *reinterpret_cast<const uint4*>(a + (size_t)gm * sam + gk)
+                                       : make_uint4(0u, 0u, 0u, 0u);
+            }
+        } else {
+            for (int idx = tid; idx < kM * kBfK; idx += kThreads) {
+                const int r = idx / kBfK, k = idx % kBfK;
+                const int gm = m0 + r, gk = k0 + k;
+                *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(sa) + bf_off(r, k)) =
+                    (gm < M && gk < K) ? a[(size_t)gm * sam + (size_t)gk * sak] : zero;
+            }
         }
-        for (int idx = tid; idx < kN * kBfK; idx += kThreads) {
-            const int n = idx / kBfK, k = idx % kBfK;
-            const int gn = n0 + n, gk = k0 + k;
-            *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(sb) + bf_off(n, k)) =
-                (gn < N && gk < K) ? b[(size_t)gk * sbk + (size_t)gn * sbn] : zero;
+        if (bvec) {
+            for (int idx = tid; idx < kN * (kBfK / 8); idx += kThreads) {
+                const int n = idx / (kBfK / 8), k = (idx % (kBfK / 8)) * 8;
+                const int gn = n0 + n, gk = k0 + k;
+                *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sb) + bf_off(n, k)) =
+                    (gn < N && gk < K) ? *reinterpret_cast<const uint4*>(b + (size_t)gn * sbn + gk)
+                                       : make_uint4(0u, 0u, 0u, 0u);
+            }
+        } else {
+            for (int idx = tid; idx < kN * kBfK; idx += kThreads) {
+                const int n = idx / kBfK, k = idx % kBfK;
+                const int gn = n0 + n, gk = k0 + k;
+                *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(sb) + bf_off(n, k)) =
+                    (gn < N && gk < K) ? b[(size_t)gk * sbk + (size_t)gn * sbn] : zero;
+            }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
